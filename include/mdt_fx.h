@@ -1,0 +1,218 @@
+/*
+ * mdt_fx.h -- C ABI of the GB300 (sm_103a) MDT FX correlator library
+ * (libmdtfx.so).
+ *
+ * Three groups of entry points, all exported with C linkage, taking plain
+ * device pointers, sizes and a cudaStream_t; no entry point aborts, all of
+ * them report errors as an mdt_status (or, for the cuFFT / cuBLAS subset, as
+ * those libraries' own status codes):
+ *
+ *  1. Drop-in reference API.  MDT_device_functions.h (this directory) keeps
+ *     the reference's three __global__ kernels with their exact signatures
+ *     (MDT_device_functions.h:44-46 of the reference); mdt_cufft_cublas_shim.h
+ *     declares the cufftPlan1d/cufftSetStream/cufftExecC2C and
+ *     cublasCreate/cublasSetStream/cublasCgemmBatched subset that the
+ *     reference client calls (MDT_OneStation_client.cu:622,630,1105,690,699,
+ *     1128), implemented on this library's own kernels.  The mdt_launch_*
+ *     functions below launch the drop-in kernels with a caller-chosen grid,
+ *     exactly as the reference client's <<<grid, block, 0, stream>>> does,
+ *     for callers (ctypes, other languages) that cannot use <<<>>>.
+ *
+ *  2. Stage entry points (mdt_fft_*, mdt_xengine_*, mdt_fengine_*): one hot
+ *     stage each, on caller-allocated device buffers.
+ *
+ *  3. The plan API (mdt_fx_*): the fused int8 F-engine + X-engine pipeline
+ *     with PFB history carried across integrations.
+ *
+ * Conventions shared by every entry point
+ *   NE      = Npols*Nelements (number of correlator inputs)
+ *   Nch     = channels per spectrum (power of two, 32..16384)
+ *   Ntaps   = PFB taps (4..128); Nsp = spectra per integration (2..16384)
+ *   int8 I/Q input    iq[(s*NE + e)*Nch + c][2]  (I then Q), the reference's
+ *                     Spectrum -> Element -> Channel order
+ *                     (MDT_device_functions.cu:172-174)
+ *   window            W[i*Nch + c], float, tap-major
+ *   F-engine output   X[(c*Nsp + s)*NE + e], complex64 (ReorderFOutput layout)
+ *   visibilities      V[c][q*NE + r] = (1/Nsp) sum_s X[c][s][r] conj(X[c][s][q]),
+ *                     complex64, column-major NE x NE per channel, full square
+ *                     (cublasCgemmBatched with OP_N, OP_C, alpha = 1/Nsp,
+ *                     MDT_OneStation_client.cu:1128, :683)
+ * Complex values are interleaved (re, im) float pairs (cuComplex layout).
+ */
+#ifndef MDT_FX_H
+#define MDT_FX_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MDT_API __attribute__((visibility("default")))
+#else
+#define MDT_API
+#endif
+
+typedef enum {
+    MDT_SUCCESS = 0,
+    MDT_ERR_INVALID_VALUE = 1, /* a size, pointer or parameter is out of range */
+    MDT_ERR_NOT_SUPPORTED = 2, /* valid request this build does not implement */
+    MDT_ERR_CUDA = 3,          /* a CUDA runtime call failed; see mdt_last_error */
+    MDT_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+    MDT_ERR_ALLOC = 5,         /* device or host allocation failed */
+    MDT_ERR_STATE = 6          /* call out of order (e.g. no window set) */
+} mdt_status;
+
+/* Parameter domain of the reference client (MDT_host_functions.h:39-46). */
+#define MDT_MIN_ELEMENTS 3
+#define MDT_MAX_ELEMENTS 2048
+#define MDT_MIN_CHANNELS 32
+#define MDT_MAX_CHANNELS 16384
+#define MDT_MIN_TAPS 4
+#define MDT_MAX_TAPS 128
+#define MDT_MIN_SPECTRA 2
+#define MDT_MAX_SPECTRA 16384
+
+/* Library version (major*1000 + minor*10 + patch). */
+MDT_API int mdt_version(void);
+/* Text of the most recent error on the calling thread ("" if none). */
+MDT_API const char *mdt_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * 1. Drop-in kernels launched with an explicit grid (as the reference client
+ *    launches them).  Each returns MDT_ERR_CUDA if the launch fails.
+ * ---------------------------------------------------------------------- */
+
+/* PFB_Window_min4term_BH (reference MDT_device_functions.cu:100-136):
+ * W[n] = sinc((n - Ntaps*Nch/2)/Nch) * minimum 4-term Blackman-Harris. */
+MDT_API mdt_status mdt_launch_PFB_Window_min4term_BH(unsigned gx, unsigned gy, unsigned gz, unsigned bx,
+    unsigned by, unsigned bz, cudaStream_t stream,
+                                                     int nchannels, int ntaps, float *window);
+
+/* PpS_Batch (reference MDT_device_functions.cu:161-209), bit-exact:
+ * NE = gz, Nsp = gy; input (Nsp+Ntaps-1) spectra of complex64. */
+MDT_API mdt_status mdt_launch_PpS_Batch(unsigned gx, unsigned gy, unsigned gz, unsigned bx,
+    unsigned by, unsigned bz, cudaStream_t stream, int nchannels,
+                                        int ntaps, float *window, void *insignal,
+                                        void *polystruct);
+
+/* ReorderFOutput (reference MDT_device_functions.cu:231-256), bit-exact:
+ * Nsp = gz; any block shape (the reference needs block (32,32)). */
+MDT_API mdt_status mdt_launch_ReorderFOutput(unsigned gx, unsigned gy, unsigned gz, unsigned bx,
+    unsigned by, unsigned bz, cudaStream_t stream,
+                                             int npolsxnelements, int nchannels, void *foutput,
+                                             void *xinput);
+
+/* Hamming windowed sinc of the benchmark configurations (no reference
+ * counterpart; the reference's window is an input array to PpS_Batch,
+ * MDT_device_functions.cu:163):
+ *   W[n] = sinc((n - Ntaps*Nch/2)/Nch) * (0.54 - 0.46 cos(2 pi n/(Ntaps*Nch))). */
+MDT_API mdt_status mdt_window_hamming_sinc(int nchannels, int ntaps, float *window,
+                                           cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 2. Stage entry points
+ * ---------------------------------------------------------------------- */
+
+/* Batched unnormalised C2C FFT over `rows` contiguous rows of n complex64
+ * (n = 2^k, 2 <= n <= 16384); in place when in == out.  direction -1 is
+ * forward (e^{-2 pi i k m/n}), +1 inverse.  Replaces cufftExecC2C
+ * (reference MDT_OneStation_client.cu:1105). */
+MDT_API mdt_status mdt_fft_c2c(const void *in, void *out, long rows, int n, int direction,
+                               cudaStream_t stream);
+
+/* Hermitian X-engine, FP32 SIMT:  for each channel c,
+ *   V_c = alpha * X_c X_c^H   (X_c = NE x Nsp column-major with leading
+ *   dimension ld >= NE, base X + c*xstride complex values), written full square
+ *   column-major with leading dimension NE at V + c*NE*NE.  Only the lower
+ *   triangle is computed; the upper is its conjugate mirror and the diagonal
+ *   is real.  Replaces cublasCgemmBatched(OP_N, OP_C, A == B)
+ *   (reference MDT_OneStation_client.cu:1128). */
+MDT_API mdt_status mdt_xengine_f32(int ne, int nch, int nsp, const void *X, long ld,
+                                   long xstride, float alpha, void *V, cudaStream_t stream);
+
+/* Fused F-engine, FP32: int8 I/Q -> PFB (fmaf in the reference's tap order)
+ * -> FFT -> channel-major complex64 X[(c*Nsp + s)*NE + e].
+ * `iq` holds Nsp + Ntaps - 1 spectra.  Bit-identical to PpS_Batch ->
+ * cufftExecC2C (this library) -> ReorderFOutput on the same samples. */
+MDT_API mdt_status mdt_fengine_f32(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                   const float *window, void *X, cudaStream_t stream);
+
+/* Deterministic synthetic int8 I/Q stream (integer-only arithmetic; same
+ * samples as the CPU generator used by the tests): spectra s0 .. s0+nsp-1,
+ * element noise sigma_q8[e]/256 LSB, optional tone table tone_q16[e][c][2]
+ * (Q16 LSB), nsrc common sources with sigma src_sigma_q8[k]/256 and integer
+ * delays src_delay[k][e] samples.  All table pointers are device pointers. */
+MDT_API mdt_status mdt_synth_iq(uint64_t seed, int ne, int nch, long s0, long nsp,
+                                const int32_t *sigma_q8, const int32_t *tone_q16, int nsrc,
+                                const int32_t *src_sigma_q8, const int32_t *src_delay,
+                                int8_t *out, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 3. Plan API: fused F-engine + X-engine with streamed PFB history
+ * ---------------------------------------------------------------------- */
+
+typedef enum {
+    MDT_PREC_FP32 = 0 /* complex64 F-output, FP32 SIMT X-engine (<=1e-5 vs FP64) */
+} mdt_precision;
+
+typedef struct {
+    int nelements; /* NE = Npols*Nelements */
+    int nchannels; /* Nch */
+    int ntaps;     /* Ntaps */
+    int nspectra;  /* Nsp per integration */
+    int precision; /* mdt_precision */
+} mdt_fx_desc;
+
+typedef struct mdt_fx_plan_s *mdt_fx_plan;
+
+/* Validates desc against the reference's parameter domain and allocates the
+ * plan's device workspace (F-engine output for one integration, the PFB
+ * history of Ntaps-1 spectra and the window). */
+MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan);
+MDT_API mdt_status mdt_fx_destroy(mdt_fx_plan plan);
+MDT_API mdt_status mdt_fx_set_stream(mdt_fx_plan plan, cudaStream_t stream);
+/* Copies Ntaps*Nch floats from a device pointer into the plan. */
+MDT_API mdt_status mdt_fx_set_window(mdt_fx_plan plan, const float *window);
+/* Bytes of device memory the plan holds. */
+MDT_API mdt_status mdt_fx_workspace_bytes(mdt_fx_plan plan, size_t *bytes);
+
+/* One-shot: iq holds nint*Nsp + Ntaps - 1 contiguous spectra (a stream with
+ * its own Ntaps-1 spectra of lead-in); writes nint integrations of
+ * visibilities V[j][c][NE*NE] complex64.  The plan's history is not used. */
+MDT_API mdt_status mdt_fx_execute(mdt_fx_plan plan, const int8_t *iq, int nint, void *vis);
+
+/* Streaming: the first call after mdt_fx_stream_reset takes Nsp + Ntaps - 1
+ * spectra (lead-in included); every later call takes Nsp new spectra and
+ * reuses the last Ntaps-1 spectra of the previous call as PFB history (the
+ * reference's device-to-device history shift, MDT_OneStation_client.cu:1170).
+ * Writes one integration of visibilities. */
+MDT_API mdt_status mdt_fx_stream_reset(mdt_fx_plan plan);
+MDT_API mdt_status mdt_fx_stream_push(mdt_fx_plan plan, const int8_t *iq, void *vis);
+
+/* Host-memory form of the streamed pipeline: h_iq (host) holds
+ * nint*Nsp + Ntaps - 1 spectra, h_vis (host) receives nint integrations.
+ * Integration j+1 is copied host->device on a second stream while j is
+ * processed and j-1's visibilities are copied back (the reference's
+ * rank 1 H2D -> rank 2 F/X -> rank 3 D2H chain, MDT_OneStation_client.cu
+ * :1048,1083-1128,1199).  Pinned host memory gives full overlap.  Allocates
+ * two input and two visibility staging buffers on first use; resets the
+ * plan's stream history; returns when the last copy has completed. */
+MDT_API mdt_status mdt_fx_execute_host(mdt_fx_plan plan, const int8_t *h_iq, int nint,
+                                       void *h_vis);
+
+/* Stage timing: when enabled, CUDA events are recorded on the plan's stream
+ * around every F-engine and X-engine launch; mdt_fx_get_timing waits for
+ * the last one, returns the summed kernel times in ms and the number of
+ * integrations, and clears the record. */
+MDT_API mdt_status mdt_fx_set_timing(mdt_fx_plan plan, int enable);
+MDT_API mdt_status mdt_fx_get_timing(mdt_fx_plan plan, double *fengine_ms, double *xengine_ms,
+                                     int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDT_FX_H */

@@ -1,0 +1,28 @@
+"""GB300-native MDT FX correlator hot path.
+
+The compute lives in libmdtfx.so (CUDA C++, sm_103a, C ABI declared in
+include/mdt_fx.h).  This package is its thin host-side binding: it loads the
+library with ctypes and exposes
+
+* the reference's drop-in interface for this path, under the reference's
+  names: PFB_Window_min4term_BH, PpS_Batch, ReorderFOutput (launched with an
+  explicit grid and block as the reference client launches them,
+  MDT_OneStation_client.cu:589,1083,1114), and the cuFFT / cuBLAS calls of
+  the same sequence (cufftPlan1d, cufftExecC2C, cublasCgemmBatched ...),
+  which resolve to this library's own kernels;
+* the stage entry points and the plan API (FxPlan) of the fused pipeline.
+
+There is no CPU fallback: if libmdtfx.so cannot be built or loaded, every
+entry point raises.  Device buffers are passed as torch CUDA tensors (or raw
+integer addresses); PyTorch is only used for device memory and streams.
+"""
+from .binding import (  # noqa: F401
+    LIB_PATH, MdtError, build, lib, check, ptr, stream_handle,
+    PFB_Window_min4term_BH, PpS_Batch, ReorderFOutput,
+    cufftPlan1d, cufftSetStream, cufftExecC2C, cufftDestroy, cufftGetVersion,
+    cublasCreate, cublasSetStream, cublasDestroy, cublasCgemmBatched,
+    CUFFT_FORWARD, CUFFT_INVERSE, CUFFT_C2C, CUBLAS_OP_N, CUBLAS_OP_T, CUBLAS_OP_C,
+    window_hamming_sinc, fft_c2c, xengine_f32, fengine_f32, synth_iq,
+    FxPlan, MDT_PREC_FP32,
+)
+from . import configs  # noqa: F401

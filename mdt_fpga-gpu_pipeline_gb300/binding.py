@@ -1,0 +1,315 @@
+"""ctypes binding of libmdtfx.so (declarations: include/mdt_fx.h,
+include/MDT_device_functions.h, include/mdt_cufft_cublas_shim.h).
+
+Every function raises MdtError on a non-success status; the cuFFT / cuBLAS
+subset raises with the library status code in MdtError.code, the way the
+reference client treats any non-success code as fatal
+(MDT_OneStation_client.cu:622-627,1130-1135).
+"""
+import ctypes
+import os
+
+from . import _build
+
+LIB_PATH = _build.LIB
+
+CUFFT_FORWARD = -1
+CUFFT_INVERSE = 1
+CUFFT_C2C = 0x29
+CUBLAS_OP_N, CUBLAS_OP_T, CUBLAS_OP_C = 0, 1, 2
+MDT_PREC_FP32 = 0
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_U = ctypes.c_uint
+_L = ctypes.c_long
+_F = ctypes.c_float
+
+_lib = None
+
+
+class MdtError(RuntimeError):
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code
+
+
+class _CuComplex(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float)]
+
+
+def build(force=False, verbose=False):
+    """Compile libmdtfx.so in-tree for sm_103a (nvcc)."""
+    return _build.build(force=force, verbose=verbose)
+
+
+def _declare(L):
+    grid6 = [_U] * 6
+    sig = {
+        "mdt_version": ([], _I),
+        "mdt_last_error": ([], ctypes.c_char_p),
+        "mdt_launch_PFB_Window_min4term_BH": (grid6 + [_P, _I, _I, _P], _I),
+        "mdt_launch_PpS_Batch": (grid6 + [_P, _I, _I, _P, _P, _P], _I),
+        "mdt_launch_ReorderFOutput": (grid6 + [_P, _I, _I, _P, _P], _I),
+        "mdt_window_hamming_sinc": ([_I, _I, _P, _P], _I),
+        "mdt_fft_c2c": ([_P, _P, _L, _I, _I, _P], _I),
+        "mdt_xengine_f32": ([_I, _I, _I, _P, _L, _L, _F, _P, _P], _I),
+        "mdt_fengine_f32": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
+        "mdt_synth_iq": ([ctypes.c_uint64, _I, _I, _L, _L, _P, _P, _I, _P, _P, _P, _P], _I),
+        "mdt_fx_create": ([_P, ctypes.POINTER(_P)], _I),
+        "mdt_fx_destroy": ([_P], _I),
+        "mdt_fx_set_stream": ([_P, _P], _I),
+        "mdt_fx_set_window": ([_P, _P], _I),
+        "mdt_fx_workspace_bytes": ([_P, ctypes.POINTER(ctypes.c_size_t)], _I),
+        "mdt_fx_execute": ([_P, _P, _I, _P], _I),
+        "mdt_fx_stream_reset": ([_P], _I),
+        "mdt_fx_stream_push": ([_P, _P, _P], _I),
+        "mdt_fx_execute_host": ([_P, _P, _I, _P], _I),
+        "mdt_fx_set_timing": ([_P, _I], _I),
+        "mdt_fx_get_timing": ([_P, ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)], _I),
+        "cufftPlan1d": ([ctypes.POINTER(_I), _I, _I, _I], _I),
+        "cufftSetStream": ([_I, _P], _I),
+        "cufftExecC2C": ([_I, _P, _P, _I], _I),
+        "cufftDestroy": ([_I], _I),
+        "cufftGetVersion": ([ctypes.POINTER(_I)], _I),
+        "cublasCreate_v2": ([ctypes.POINTER(_P)], _I),
+        "cublasDestroy_v2": ([_P], _I),
+        "cublasSetStream_v2": ([_P, _P], _I),
+        "cublasGetStream_v2": ([_P, ctypes.POINTER(_P)], _I),
+        "cublasCgemmBatched": ([_P, _I, _I, _I, _I, _I, ctypes.POINTER(_CuComplex), _P, _I, _P,
+                                _I, ctypes.POINTER(_CuComplex), _P, _I, _I], _I),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+
+
+def lib():
+    """The loaded libmdtfx.so; builds it first if it is missing or stale."""
+    global _lib
+    if _lib is None:
+        if not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise MdtError("libmdtfx.so is missing and could not be built")
+        L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def check(status, what):
+    if status != 0:
+        msg = lib().mdt_last_error().decode(errors="replace")
+        raise MdtError("%s failed (mdt_status %d): %s" % (what, status, msg), status)
+
+
+def ptr(x):
+    """Device address of a torch tensor / integer / None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if hasattr(x, "is_cuda") and not x.is_cuda:
+            raise MdtError("expected a CUDA tensor")
+        return x.data_ptr()
+    raise TypeError("cannot take a device address of %r" % type(x))
+
+
+def _host_ptr(x):
+    if hasattr(x, "ctypes"):
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return int(x)
+
+
+def stream_handle(stream=None):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _g6(grid, block):
+    g = tuple(grid) + (1,) * (3 - len(grid))
+    b = tuple(block) + (1,) * (3 - len(block))
+    return list(g) + list(b)
+
+
+# ----------------------------------------------------------- drop-in kernels
+def PFB_Window_min4term_BH(grid, block, Nchannels, Ntaps, Window, stream=None):
+    check(lib().mdt_launch_PFB_Window_min4term_BH(*_g6(grid, block), stream_handle(stream),
+                                                  Nchannels, Ntaps, ptr(Window)),
+          "PFB_Window_min4term_BH")
+
+
+def PpS_Batch(grid, block, Nchannels, Ntaps, Window, InSignal, PolyStruct, stream=None):
+    check(lib().mdt_launch_PpS_Batch(*_g6(grid, block), stream_handle(stream), Nchannels, Ntaps,
+                                     ptr(Window), ptr(InSignal), ptr(PolyStruct)), "PpS_Batch")
+
+
+def ReorderFOutput(grid, block, NpolsxNelements, Nchannels, FOutput, XInput, stream=None):
+    check(lib().mdt_launch_ReorderFOutput(*_g6(grid, block), stream_handle(stream),
+                                          NpolsxNelements, Nchannels, ptr(FOutput), ptr(XInput)),
+          "ReorderFOutput")
+
+
+# ----------------------------------------------------------- cuFFT subset
+def _cufft(rc, what):
+    if rc != 0:
+        raise MdtError("%s returned cufftResult %d" % (what, rc), rc)
+
+
+def cufftPlan1d(nx, fft_type, batch):
+    h = _I(0)
+    _cufft(lib().cufftPlan1d(ctypes.byref(h), nx, fft_type, batch), "cufftPlan1d")
+    return h.value
+
+
+def cufftSetStream(plan, stream):
+    _cufft(lib().cufftSetStream(plan, stream_handle(stream)), "cufftSetStream")
+
+
+def cufftExecC2C(plan, idata, odata, direction):
+    _cufft(lib().cufftExecC2C(plan, ptr(idata), ptr(odata), direction), "cufftExecC2C")
+
+
+def cufftDestroy(plan):
+    _cufft(lib().cufftDestroy(plan), "cufftDestroy")
+
+
+def cufftGetVersion():
+    v = _I(0)
+    _cufft(lib().cufftGetVersion(ctypes.byref(v)), "cufftGetVersion")
+    return v.value
+
+
+# ----------------------------------------------------------- cuBLAS subset
+def _cublas(rc, what):
+    if rc != 0:
+        raise MdtError("%s returned cublasStatus %d" % (what, rc), rc)
+
+
+def cublasCreate():
+    h = _P()
+    _cublas(lib().cublasCreate_v2(ctypes.byref(h)), "cublasCreate")
+    return h.value
+
+
+def cublasSetStream(handle, stream):
+    _cublas(lib().cublasSetStream_v2(handle, stream_handle(stream)), "cublasSetStream")
+
+
+def cublasDestroy(handle):
+    _cublas(lib().cublasDestroy_v2(handle), "cublasDestroy")
+
+
+def cublasCgemmBatched(handle, transa, transb, m, n, k, alpha, Aarray, lda, Barray, ldb, beta,
+                       Carray, ldc, batchCount):
+    """Aarray/Barray/Carray: device arrays of device pointers (e.g. int64 CUDA
+    tensors); alpha/beta: Python complex numbers (host pointer mode)."""
+    a = _CuComplex(complex(alpha).real, complex(alpha).imag)
+    b = _CuComplex(complex(beta).real, complex(beta).imag)
+    _cublas(lib().cublasCgemmBatched(handle, transa, transb, m, n, k, ctypes.byref(a),
+                                     ptr(Aarray), lda, ptr(Barray), ldb, ctypes.byref(b),
+                                     ptr(Carray), ldc, batchCount), "cublasCgemmBatched")
+
+
+# ----------------------------------------------------------- stage entry points
+def window_hamming_sinc(nchannels, ntaps, window, stream=None):
+    check(lib().mdt_window_hamming_sinc(nchannels, ntaps, ptr(window), stream_handle(stream)),
+          "window_hamming_sinc")
+
+
+def fft_c2c(inp, out, rows, n, direction=CUFFT_FORWARD, stream=None):
+    check(lib().mdt_fft_c2c(ptr(inp), ptr(out), rows, n, direction, stream_handle(stream)),
+          "fft_c2c")
+
+
+def xengine_f32(ne, nch, nsp, X, ld, xstride, alpha, V, stream=None):
+    check(lib().mdt_xengine_f32(ne, nch, nsp, ptr(X), ld, xstride, alpha, ptr(V),
+                                stream_handle(stream)), "xengine_f32")
+
+
+def fengine_f32(ne, nch, ntaps, nsp, iq, window, X, stream=None):
+    check(lib().mdt_fengine_f32(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X),
+                                stream_handle(stream)), "fengine_f32")
+
+
+def synth_iq(seed, ne, nch, s0, nsp, sigma_q8, out, tone_q16=None, src_sigma_q8=None,
+             src_delay=None, stream=None):
+    nsrc = 0 if src_sigma_q8 is None else int(src_sigma_q8.numel())
+    check(lib().mdt_synth_iq(seed, ne, nch, s0, nsp, ptr(sigma_q8), ptr(tone_q16), nsrc,
+                             ptr(src_sigma_q8), ptr(src_delay), ptr(out), stream_handle(stream)),
+          "synth_iq")
+
+
+# ----------------------------------------------------------- plan API
+class _Desc(ctypes.Structure):
+    _fields_ = [("nelements", _I), ("nchannels", _I), ("ntaps", _I), ("nspectra", _I),
+                ("precision", _I)]
+
+
+class FxPlan:
+    """Fused F-engine + X-engine plan (mdt_fx_*)."""
+
+    def __init__(self, nelements, nchannels, ntaps, nspectra, precision=MDT_PREC_FP32,
+                 stream=None):
+        self.ne, self.nch, self.ntaps, self.nsp = nelements, nchannels, ntaps, nspectra
+        d = _Desc(nelements, nchannels, ntaps, nspectra, precision)
+        h = _P()
+        check(lib().mdt_fx_create(ctypes.byref(d), ctypes.byref(h)), "mdt_fx_create")
+        self._h = h
+        self.set_stream(stream)
+
+    def set_stream(self, stream=None):
+        check(lib().mdt_fx_set_stream(self._h, stream_handle(stream)), "mdt_fx_set_stream")
+
+    def set_window(self, window):
+        check(lib().mdt_fx_set_window(self._h, ptr(window)), "mdt_fx_set_window")
+
+    def workspace_bytes(self):
+        v = ctypes.c_size_t(0)
+        check(lib().mdt_fx_workspace_bytes(self._h, ctypes.byref(v)), "mdt_fx_workspace_bytes")
+        return v.value
+
+    def execute(self, iq, nint, vis):
+        check(lib().mdt_fx_execute(self._h, ptr(iq), nint, ptr(vis)), "mdt_fx_execute")
+
+    def stream_reset(self):
+        check(lib().mdt_fx_stream_reset(self._h), "mdt_fx_stream_reset")
+
+    def stream_push(self, iq, vis):
+        check(lib().mdt_fx_stream_push(self._h, ptr(iq), ptr(vis)), "mdt_fx_stream_push")
+
+    def execute_host(self, h_iq, nint, h_vis):
+        """h_iq / h_vis: host buffers (numpy arrays or pinned torch CPU tensors)."""
+        check(lib().mdt_fx_execute_host(self._h, _host_ptr(h_iq), nint, _host_ptr(h_vis)),
+              "mdt_fx_execute_host")
+
+    def set_timing(self, enable=True):
+        check(lib().mdt_fx_set_timing(self._h, 1 if enable else 0), "mdt_fx_set_timing")
+
+    def get_timing(self):
+        """(F-engine ms, X-engine ms, integrations) recorded since set_timing."""
+        f, x, n = ctypes.c_double(0), ctypes.c_double(0), _I(0)
+        check(lib().mdt_fx_get_timing(self._h, ctypes.byref(f), ctypes.byref(x), ctypes.byref(n)),
+              "mdt_fx_get_timing")
+        return f.value, x.value, n.value
+
+    def close(self):
+        if self._h:
+            check(lib().mdt_fx_destroy(self._h), "mdt_fx_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

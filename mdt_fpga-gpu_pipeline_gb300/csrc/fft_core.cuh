@@ -1,0 +1,182 @@
+// fft_core.cuh -- shared-memory Stockham FFT core (forward, unnormalised,
+// natural order in and out), used by the standalone batched FFT (the
+// cufftExecC2C replacement) and by the fused F-engine.
+//
+// One row of N = 2^L complex values is transformed by TPR threads through
+// L/3 radix-8 passes and, when L is not a multiple of 3, one final radix-2
+// or radix-4 pass.  Pass p (radix R, NS = 8^p) on butterfly b:
+//   v[m]  = x[b + m*N/R]                              m = 0..R-1
+//   v[m] *= exp(-2 pi i m (b mod NS) / (NS*R))        (table lookup)
+//   v     = DFT_R(v)
+//   y[(b/NS)*NS*R + (b mod NS) + m*NS] = v[m]
+// which is the self-sorting (Stockham) formulation: the first pass reads the
+// row in natural order and the last pass writes it in natural order, so the
+// first pass can take its inputs from any producer (global memory, the PFB
+// tap sum) and the last pass can hand its outputs to any consumer.
+// Intermediate passes exchange through shared memory, real and imaginary
+// parts in separate padded arrays (index i + i/8) to spread banks.
+// All arithmetic uses explicitly rounded intrinsics so every instantiation
+// of the core produces bit-identical results.
+#pragma once
+#include "mdt_common.cuh"
+
+namespace mdt {
+namespace fft {
+
+constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
+constexpr int ipow8(int p) { return p == 0 ? 1 : 8 * ipow8(p - 1); }
+
+__host__ __device__ constexpr int pad(int i) { return i + (i >> 3); }
+
+template <int N>
+struct Shape {
+    static constexpr int L = clog2(N);
+    static constexpr int P8 = L / 3;     // radix-8 passes
+    static constexpr int REM = L % 3;    // final radix-2^REM pass if REM > 0
+    static constexpr int NPASS = P8 + (REM ? 1 : 0);
+    static constexpr int TPR = (N / 8 < 1) ? 1 : ((N / 8 > 1024) ? 1024 : N / 8);  // threads per row
+    static constexpr int PADN = pad(N);  // floats per padded real or imag array
+};
+
+constexpr float kRsqrt2 = 0.70710678118654752440f;
+
+template <int R>
+__device__ __forceinline__ void dft(float2 *v);
+
+template <>
+__device__ __forceinline__ void dft<1>(float2 *)
+{
+}
+
+template <>
+__device__ __forceinline__ void dft<2>(float2 *v)
+{
+    float2 a = cadd(v[0], v[1]), b = csub(v[0], v[1]);
+    v[0] = a;
+    v[1] = b;
+}
+
+// y_k = sum_n x_n (-i)^{nk}
+__device__ __forceinline__ void dft4v(float2 &x0, float2 &x1, float2 &x2, float2 &x3)
+{
+    float2 c0 = cadd(x0, x2), c1 = csub(x0, x2);
+    float2 c2 = cadd(x1, x3), c3 = cmul_mi(csub(x1, x3));
+    x0 = cadd(c0, c2);
+    x1 = cadd(c1, c3);
+    x2 = csub(c0, c2);
+    x3 = csub(c1, c3);
+}
+
+template <>
+__device__ __forceinline__ void dft<4>(float2 *v)
+{
+    dft4v(v[0], v[1], v[2], v[3]);
+}
+
+// Radix-8 by one decimation-in-frequency split into two radix-4 DFTs:
+//   y_{2k}   = DFT4(v_n + v_{n+4})_k
+//   y_{2k+1} = DFT4((v_n - v_{n+4}) W8^n)_k,   W8 = exp(-2 pi i/8)
+template <>
+__device__ __forceinline__ void dft<8>(float2 *v)
+{
+    float2 a0 = cadd(v[0], v[4]), a1 = cadd(v[1], v[5]), a2 = cadd(v[2], v[6]),
+           a3 = cadd(v[3], v[7]);
+    float2 b0 = csub(v[0], v[4]), b1 = csub(v[1], v[5]), b2 = csub(v[2], v[6]),
+           b3 = csub(v[3], v[7]);
+    // b1 *= (1 - i)/sqrt2 ; b2 *= -i ; b3 *= (-1 - i)/sqrt2
+    b1 = make_float2(__fmul_rn(__fadd_rn(b1.x, b1.y), kRsqrt2),
+                     __fmul_rn(__fsub_rn(b1.y, b1.x), kRsqrt2));
+    b2 = cmul_mi(b2);
+    b3 = make_float2(__fmul_rn(__fsub_rn(b3.y, b3.x), kRsqrt2),
+                     -__fmul_rn(__fadd_rn(b3.x, b3.y), kRsqrt2));
+    dft4v(a0, a1, a2, a3);
+    dft4v(b0, b1, b2, b3);
+    v[0] = a0; v[2] = a1; v[4] = a2; v[6] = a3;
+    v[1] = b0; v[3] = b1; v[5] = b2; v[7] = b3;
+}
+
+// One Stockham pass over one row.  `t` is the thread's index within the row
+// (0..TPR-1); every thread of the block must call every pass (barriers).
+// FIRST: inputs come from load(i); otherwise from shared memory.
+// LAST : outputs go to store(i, v); otherwise to shared memory.
+template <int N, int TPR, int P, bool FIRST, bool LAST, class Load, class Store>
+__device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
+                                              const float2 *__restrict__ tw, Load &load,
+                                              Store &store)
+{
+    constexpr int R = (P < Shape<N>::P8) ? 8 : (1 << Shape<N>::REM);
+    constexpr int NS = ipow8(P);
+    constexpr int NB = N / R;
+    constexpr int NBT = (NB + TPR - 1) / TPR;
+    float2 v[NBT][R];
+#pragma unroll
+    for (int k = 0; k < NBT; k++) {
+        const int b = t + k * TPR;
+        if (NBT * TPR == NB || b < NB) {
+#pragma unroll
+            for (int m = 0; m < R; m++) {
+                const int idx = b + m * NB;
+                if constexpr (FIRST) {
+                    v[k][m] = load(idx);
+                } else {
+                    v[k][m] = make_float2(sre[pad(idx)], sim[pad(idx)]);
+                }
+            }
+            if constexpr (NS > 1) {
+                const int jm = b & (NS - 1);
+#pragma unroll
+                for (int m = 1; m < R; m++)
+                    v[k][m] = cmul(v[k][m], __ldg(&tw[m * jm * (N / (NS * R))]));
+            }
+            dft<R>(v[k]);
+        }
+    }
+    if constexpr (!FIRST) __syncthreads();  // every read of this pass precedes any write
+#pragma unroll
+    for (int k = 0; k < NBT; k++) {
+        const int b = t + k * TPR;
+        if (NBT * TPR == NB || b < NB) {
+            const int base = (b / NS) * NS * R + (b & (NS - 1));
+#pragma unroll
+            for (int m = 0; m < R; m++) {
+                const int o = base + m * NS;
+                if constexpr (LAST) {
+                    store(o, v[k][m]);
+                } else {
+                    sre[pad(o)] = v[k][m].x;
+                    sim[pad(o)] = v[k][m].y;
+                }
+            }
+        }
+    }
+    if constexpr (!LAST) __syncthreads();  // writes visible to the next pass
+}
+
+template <int N, int TPR, int P, class Load, class Store>
+__device__ __forceinline__ void run_passes(float *sre, float *sim, int t,
+                                           const float2 *__restrict__ tw, Load &load,
+                                           Store &store)
+{
+    constexpr int NP = Shape<N>::NPASS;
+    stockham_pass<N, TPR, P, P == 0, P == NP - 1>(sre, sim, t, tw, load, store);
+    if constexpr (P + 1 < NP) run_passes<N, TPR, P + 1>(sre, sim, t, tw, load, store);
+}
+
+// Transforms one row: first-pass inputs from load(i), natural-order outputs
+// to store(i, v).  sre/sim: this row's shared arrays of Shape<N>::PADN floats.
+template <int N, int TPR, class Load, class Store>
+__device__ __forceinline__ void transform_row(float *sre, float *sim, int t,
+                                              const float2 *__restrict__ tw, Load &load,
+                                              Store &store)
+{
+    run_passes<N, TPR, 0>(sre, sim, t, tw, load, store);
+}
+
+}  // namespace fft
+
+// Device twiddle table exp(-2 pi i k / n), k < n, built in double on the host
+// on first use per (device, n) and kept until process exit.  Must be called
+// outside stream capture the first time for a given n.
+const float2 *fft_twiddles(int n, mdt_status *st);
+
+}  // namespace mdt

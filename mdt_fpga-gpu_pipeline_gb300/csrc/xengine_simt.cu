@@ -1,0 +1,404 @@
+// xengine_simt.cu -- FP32 (SIMT) X-engine: per channel c the Hermitian
+// product V_c = alpha * X_c X_c^H (+ beta V_c), computed on the lower
+// triangle only and mirrored, which is the reference's cublasCgemmBatched
+// call (OP_N, OP_C, A == B, alpha = 1/Nspectra, beta = 0;
+// MDT_OneStation_client.cu:1128, :656-660, :683-686).  Also the cuBLAS
+// subset the reference calls (cublasCreate/cublasSetStream/cublasDestroy/
+// cublasCgemmBatched, :690,:699,:1128), with a general batched CGEMM for
+// argument patterns other than the Hermitian one.
+//
+// Tiling: a block owns one pair (I >= J) of 64-wide super-tiles of one
+// channel; each thread accumulates a 4x4 complex micro-tile.  Only micro-tiles
+// on or below the diagonal are computed in diagonal pairs.  When a pair has
+// fewer than 256 micro-tiles the spare threads split the K (time) loop and
+// the partial sums are added in a fixed order.
+#include <cublas_v2.h>
+#include "mdt_cufft_cublas_shim.h"  // checks the exported signatures
+
+#include <algorithm>
+#include <new>
+
+#include "mdt_common.cuh"
+
+namespace mdt {
+
+constexpr int XS_ST = 64;       // super-tile width
+constexpr int XS_MT = 4;        // micro-tile width
+constexpr int XS_KC = 32;       // time samples staged per chunk
+constexpr int XS_THREADS = 256;
+
+struct XengArgs {
+    int ne, nsp, nsuper, npairs;
+    const float2 *X;             // base (when Xptrs == nullptr)
+    const float2 *const *Xptrs;  // per-channel operand pointers (cuBLAS shim)
+    long ld, xstride;
+    float2 *V;
+    float2 *const *Vptrs;
+    long ldv, vstride;
+    float2 alpha, beta;
+    int beta_zero;
+};
+
+__device__ __forceinline__ void pair_index(int p, int &I, int &J)
+{
+    // p enumerates (I, J), I >= J, row by row: p = I(I+1)/2 + J
+    int i = (int)((sqrtf(8.0f * p + 1.0f) - 1.0f) * 0.5f);
+    while ((i + 1) * (i + 2) / 2 <= p) i++;
+    while (i * (i + 1) / 2 > p) i--;
+    I = i;
+    J = p - i * (i + 1) / 2;
+}
+
+__global__ void __launch_bounds__(XS_THREADS) xengine_herm_f32_kernel(XengArgs a)
+{
+    // one array so that the K-slice reduction can reuse both operand tiles
+    __shared__ __align__(16) float2 sbuf[2][XS_KC][XS_ST];
+    float2(*sA)[XS_ST] = sbuf[0];
+    float2(*sB)[XS_ST] = sbuf[1];
+
+    const int ch = blockIdx.x / a.npairs;
+    const int pr = blockIdx.x - ch * a.npairs;
+    int I, J;
+    pair_index(pr, I, J);
+    const bool diag = (I == J);
+    const int r0 = I * XS_ST, q0 = J * XS_ST;
+    const int nr = min(XS_ST, a.ne - r0), nq = min(XS_ST, a.ne - q0);
+    const int nmr = (nr + XS_MT - 1) / XS_MT, nmq = (nq + XS_MT - 1) / XS_MT;
+    const int nmt = diag ? nmr * (nmr + 1) / 2 : nmr * nmq;
+    const int ksl = min(XS_KC, max(1, XS_THREADS / nmt));
+    const int tid = threadIdx.x;
+    const bool active = tid < nmt * ksl;
+    const int mt = tid % nmt, ks = tid / nmt;
+    int mi, mj;
+    if (diag) {
+        pair_index(mt, mi, mj);
+    } else {
+        mi = mt / nmq;
+        mj = mt - mi * nmq;
+    }
+
+    const float2 *Xc = a.Xptrs ? a.Xptrs[ch] : a.X + (long)ch * a.xstride;
+
+    float2 acc[XS_MT][XS_MT];
+#pragma unroll
+    for (int i = 0; i < XS_MT; i++)
+#pragma unroll
+        for (int j = 0; j < XS_MT; j++) acc[i][j] = make_float2(0.f, 0.f);
+
+    // staging: XS_KC x 64 complex per operand, 8 per thread
+    constexpr int PER = XS_KC * XS_ST / XS_THREADS;
+    float2 ra[PER], rb[PER];
+    auto fetch = [&](int k0) {
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            int idx = tid + u * XS_THREADS;
+            int kk = idx / XS_ST, e = idx - kk * XS_ST;
+            int k = k0 + kk;
+            bool kin = k < a.nsp;
+            ra[u] = (kin && e < nr) ? Xc[(long)k * a.ld + r0 + e] : make_float2(0.f, 0.f);
+            if (!diag) rb[u] = (kin && e < nq) ? Xc[(long)k * a.ld + q0 + e] : make_float2(0.f, 0.f);
+        }
+    };
+    auto stash = [&]() {
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            int idx = tid + u * XS_THREADS;
+            int kk = idx / XS_ST, e = idx - kk * XS_ST;
+            sA[kk][e] = ra[u];
+            if (!diag) sB[kk][e] = rb[u];
+        }
+    };
+
+    const float2(*B)[XS_ST] = diag ? sA : sB;
+    fetch(0);
+    for (int k0 = 0; k0 < a.nsp; k0 += XS_KC) {
+        __syncthreads();
+        stash();
+        __syncthreads();
+        if (k0 + XS_KC < a.nsp) fetch(k0 + XS_KC);
+        if (active) {
+            for (int kk = ks; kk < XS_KC; kk += ksl) {
+                const float4 *pa = reinterpret_cast<const float4 *>(&sA[kk][mi * XS_MT]);
+                const float4 *pb = reinterpret_cast<const float4 *>(&B[kk][mj * XS_MT]);
+                float4 a01 = pa[0], a23 = pa[1], b01 = pb[0], b23 = pb[1];
+                float2 av[4] = {make_float2(a01.x, a01.y), make_float2(a01.z, a01.w),
+                                make_float2(a23.x, a23.y), make_float2(a23.z, a23.w)};
+                float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w),
+                                make_float2(b23.x, b23.y), make_float2(b23.z, b23.w)};
+#pragma unroll
+                for (int i = 0; i < XS_MT; i++)
+#pragma unroll
+                    for (int j = 0; j < XS_MT; j++) {
+                        // acc += a * conj(b)
+                        acc[i][j].x = fmaf(av[i].x, bv[j].x, acc[i][j].x);
+                        acc[i][j].x = fmaf(av[i].y, bv[j].y, acc[i][j].x);
+                        acc[i][j].y = fmaf(av[i].y, bv[j].x, acc[i][j].y);
+                        acc[i][j].y = fmaf(-av[i].x, bv[j].y, acc[i][j].y);
+                    }
+            }
+        }
+    }
+
+    // reduce the K slices in a fixed order (slice 0 + 1 + 2 ...)
+    if (ksl > 1) {
+        __syncthreads();
+        float2 *red = &sbuf[0][0][0];  // (ksl-1)*nmt*16 < 256*16 complex = both tiles
+        if (active && ks > 0) {
+#pragma unroll
+            for (int i = 0; i < XS_MT; i++)
+#pragma unroll
+                for (int j = 0; j < XS_MT; j++) red[((ks - 1) * nmt + mt) * 16 + i * 4 + j] = acc[i][j];
+        }
+        __syncthreads();
+        if (active && ks == 0) {
+            for (int s2 = 1; s2 < ksl; s2++) {
+#pragma unroll
+                for (int i = 0; i < XS_MT; i++)
+#pragma unroll
+                    for (int j = 0; j < XS_MT; j++) {
+                        float2 v = red[((s2 - 1) * nmt + mt) * 16 + i * 4 + j];
+                        acc[i][j].x += v.x;
+                        acc[i][j].y += v.y;
+                    }
+            }
+        }
+    }
+    if (!active || ks != 0) return;
+
+    float2 *Vc = a.Vptrs ? a.Vptrs[ch] : a.V + (long)ch * a.vstride;
+#pragma unroll
+    for (int i = 0; i < XS_MT; i++) {
+#pragma unroll
+        for (int j = 0; j < XS_MT; j++) {
+            const int r = r0 + mi * XS_MT + i, q = q0 + mj * XS_MT + j;
+            if (r >= a.ne || q >= a.ne || r < q) continue;
+            float2 v = acc[i][j];
+            if (r == q) v.y = 0.f;  // autocorrelations are real
+            // lower:  V[r,q] = alpha v + beta V[r,q]
+            float2 lo = make_float2(a.alpha.x * v.x - a.alpha.y * v.y,
+                                    a.alpha.x * v.y + a.alpha.y * v.x);
+            long il = (long)q * a.ldv + r;
+            if (!a.beta_zero) {
+                float2 o = Vc[il];
+                lo.x += a.beta.x * o.x - a.beta.y * o.y;
+                lo.y += a.beta.x * o.y + a.beta.y * o.x;
+            }
+            Vc[il] = lo;
+            if (r != q) {
+                // upper mirror: V[q,r] = alpha conj(v) + beta V[q,r]
+                float2 up = make_float2(a.alpha.x * v.x + a.alpha.y * v.y,
+                                        -a.alpha.x * v.y + a.alpha.y * v.x);
+                long iu = (long)r * a.ldv + q;
+                if (!a.beta_zero) {
+                    float2 o = Vc[iu];
+                    up.x += a.beta.x * o.x - a.beta.y * o.y;
+                    up.y += a.beta.x * o.y + a.beta.y * o.x;
+                }
+                Vc[iu] = up;
+            }
+        }
+    }
+}
+
+mdt_status xengine_herm_f32(int ne, long nbatch, int nsp, const float2 *X,
+                            const float2 *const *Xptrs, long ld, long xstride, float2 *V,
+                            float2 *const *Vptrs, long ldv, long vstride, float2 alpha,
+                            float2 beta, bool beta_zero, cudaStream_t stream)
+{
+    if (ne <= 0 || nbatch <= 0) return MDT_SUCCESS;
+    XengArgs a;
+    a.ne = ne;
+    a.nsp = nsp;
+    a.nsuper = (int)cdiv(ne, XS_ST);
+    a.npairs = a.nsuper * (a.nsuper + 1) / 2;
+    a.X = X;
+    a.Xptrs = Xptrs;
+    a.ld = ld;
+    a.xstride = xstride;
+    a.V = V;
+    a.Vptrs = Vptrs;
+    a.ldv = ldv;
+    a.vstride = vstride;
+    a.alpha = alpha;
+    a.beta = beta;
+    a.beta_zero = beta_zero ? 1 : 0;
+    long blocks = nbatch * a.npairs;
+    if (blocks > 0x7fffffffL) return invalid("xengine: grid too large");
+    xengine_herm_f32_kernel<<<(unsigned)blocks, XS_THREADS, 0, stream>>>(a);
+    return launch_status("xengine_herm_f32_kernel");
+}
+
+// ---------------------------------------------------- general batched CGEMM
+// C = alpha op(A) op(B) + beta C, column-major, 16x16 tiles; for the cuBLAS
+// argument patterns that are not the Hermitian X-engine.
+struct GemmArgs {
+    int m, n, k, ta, tb;  // 0 = N, 1 = T, 2 = C
+    const float2 *const *A;
+    const float2 *const *B;
+    float2 *const *C;
+    int lda, ldb, ldc;
+    float2 alpha, beta;
+    int beta_zero;
+};
+
+__device__ __forceinline__ float2 opval(const float2 *M, int ld, int t, int row, int col)
+{
+    // element (row, col) of op(M)
+    float2 v = (t == 0) ? M[(long)col * ld + row] : M[(long)row * ld + col];
+    if (t == 2) v.y = -v.y;
+    return v;
+}
+
+__global__ void cgemm_batched_kernel(GemmArgs g)
+{
+    __shared__ float2 sa[16][17], sb[16][17];
+    const int b = blockIdx.z;
+    const float2 *A = g.A[b], *B = g.B[b];
+    float2 *C = g.C[b];
+    const int i = blockIdx.x * 16 + threadIdx.x, j = blockIdx.y * 16 + threadIdx.y;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int l0 = 0; l0 < g.k; l0 += 16) {
+        int ar = blockIdx.x * 16 + threadIdx.x, ac = l0 + threadIdx.y;
+        sa[threadIdx.y][threadIdx.x] =
+            (ar < g.m && ac < g.k) ? opval(A, g.lda, g.ta, ar, ac) : make_float2(0.f, 0.f);
+        int br = l0 + threadIdx.x, bc = blockIdx.y * 16 + threadIdx.y;
+        sb[threadIdx.y][threadIdx.x] =
+            (br < g.k && bc < g.n) ? opval(B, g.ldb, g.tb, br, bc) : make_float2(0.f, 0.f);
+        __syncthreads();
+#pragma unroll
+        for (int l = 0; l < 16; l++) {
+            float2 x = sa[l][threadIdx.x], y = sb[threadIdx.y][l];
+            acc.x = fmaf(x.x, y.x, acc.x);
+            acc.x = fmaf(-x.y, y.y, acc.x);
+            acc.y = fmaf(x.x, y.y, acc.y);
+            acc.y = fmaf(x.y, y.x, acc.y);
+        }
+        __syncthreads();
+    }
+    if (i < g.m && j < g.n) {
+        float2 r = make_float2(g.alpha.x * acc.x - g.alpha.y * acc.y,
+                               g.alpha.x * acc.y + g.alpha.y * acc.x);
+        long ic = (long)j * g.ldc + i;
+        if (!g.beta_zero) {
+            float2 o = C[ic];
+            r.x += g.beta.x * o.x - g.beta.y * o.y;
+            r.y += g.beta.x * o.y + g.beta.y * o.x;
+        }
+        C[ic] = r;
+    }
+}
+
+}  // namespace mdt
+
+// ---------------------------------------------------------------- C ABI
+extern "C" {
+
+MDT_API mdt_status mdt_xengine_f32(int ne, int nch, int nsp, const void *X, long ld,
+                                   long xstride, float alpha, void *V, cudaStream_t stream)
+{
+    if (!X || !V || ne <= 0 || nch < 0 || nsp < 0 || ld < ne)
+        return mdt::invalid("xengine_f32: bad arguments");
+    return mdt::xengine_herm_f32(ne, nch, nsp, (const float2 *)X, nullptr, ld, xstride,
+                                 (float2 *)V, nullptr, ne, (long)ne * ne,
+                                 make_float2(alpha, 0.f), make_float2(0.f, 0.f), true, stream);
+}
+
+}  // extern "C"
+
+// cuBLAS handle of the shim: only the stream is kept.
+struct cublasContext {
+    unsigned magic;
+    cudaStream_t stream;
+};
+static const unsigned kShimMagic = 0x4d445446u;  // "MDTF"
+
+extern "C" {
+
+// cublasCreate (reference MDT_OneStation_client.cu:690)
+cublasStatus_t CUBLASWINAPI cublasCreate_v2(cublasHandle_t *handle)
+{
+    if (!handle) return CUBLAS_STATUS_INVALID_VALUE;
+    cublasContext *c = new (std::nothrow) cublasContext;
+    if (!c) return CUBLAS_STATUS_ALLOC_FAILED;
+    c->magic = kShimMagic;
+    c->stream = 0;
+    *handle = c;
+    return CUBLAS_STATUS_SUCCESS;
+}
+
+cublasStatus_t CUBLASWINAPI cublasDestroy_v2(cublasHandle_t handle)
+{
+    if (!handle || handle->magic != kShimMagic) return CUBLAS_STATUS_NOT_INITIALIZED;
+    handle->magic = 0;
+    delete handle;
+    return CUBLAS_STATUS_SUCCESS;
+}
+
+// cublasSetStream (reference :699)
+cublasStatus_t CUBLASWINAPI cublasSetStream_v2(cublasHandle_t handle, cudaStream_t streamId)
+{
+    if (!handle || handle->magic != kShimMagic) return CUBLAS_STATUS_NOT_INITIALIZED;
+    handle->stream = streamId;
+    return CUBLAS_STATUS_SUCCESS;
+}
+
+cublasStatus_t CUBLASWINAPI cublasGetStream_v2(cublasHandle_t handle, cudaStream_t *streamId)
+{
+    if (!handle || handle->magic != kShimMagic) return CUBLAS_STATUS_NOT_INITIALIZED;
+    if (!streamId) return CUBLAS_STATUS_INVALID_VALUE;
+    *streamId = handle->stream;
+    return CUBLAS_STATUS_SUCCESS;
+}
+
+// cublasCgemmBatched (reference :1128).  alpha/beta are host pointers (the
+// default pointer mode).  transa = N, transb = C, m == n, Aarray == Barray,
+// lda == ldb selects the Hermitian X-engine; any other pattern runs the
+// general batched CGEMM.
+cublasStatus_t CUBLASWINAPI cublasCgemmBatched(cublasHandle_t handle, cublasOperation_t transa,
+                                               cublasOperation_t transb, int m, int n, int k,
+                                               const cuComplex *alpha,
+                                               const cuComplex *const Aarray[], int lda,
+                                               const cuComplex *const Barray[], int ldb,
+                                               const cuComplex *beta,
+                                               cuComplex *const Carray[], int ldc,
+                                               int batchCount)
+{
+    if (!handle || handle->magic != kShimMagic) return CUBLAS_STATUS_NOT_INITIALIZED;
+    auto opcode = [](cublasOperation_t t) {
+        return t == CUBLAS_OP_N ? 0 : t == CUBLAS_OP_T ? 1 : t == CUBLAS_OP_C ? 2 : -1;
+    };
+    int ta = opcode(transa), tb = opcode(transb);
+    if (ta < 0 || tb < 0) return CUBLAS_STATUS_INVALID_VALUE;
+    if (m < 0 || n < 0 || k < 0 || batchCount < 0 || !alpha || !beta)
+        return CUBLAS_STATUS_INVALID_VALUE;
+    if (lda < std::max(1, ta == 0 ? m : k) || ldb < std::max(1, tb == 0 ? k : n) ||
+        ldc < std::max(1, m))
+        return CUBLAS_STATUS_INVALID_VALUE;
+    if (m == 0 || n == 0 || batchCount == 0) return CUBLAS_STATUS_SUCCESS;
+    if (!Aarray || !Barray || !Carray) return CUBLAS_STATUS_INVALID_VALUE;
+    float2 al = make_float2(alpha->x, alpha->y), be = make_float2(beta->x, beta->y);
+    bool beta_zero = (be.x == 0.f && be.y == 0.f);
+    mdt_status st;
+    if (ta == 0 && tb == 2 && m == n && (const void *)Aarray == (const void *)Barray &&
+        lda == ldb) {
+        st = mdt::xengine_herm_f32(m, batchCount, k, nullptr,
+                                   reinterpret_cast<const float2 *const *>(Aarray), lda, 0,
+                                   nullptr, reinterpret_cast<float2 *const *>(Carray), ldc, 0,
+                                   al, be, beta_zero, handle->stream);
+    } else {
+        if (batchCount > 65535) return CUBLAS_STATUS_NOT_SUPPORTED;
+        mdt::GemmArgs g;
+        g.m = m; g.n = n; g.k = k; g.ta = ta; g.tb = tb;
+        g.A = reinterpret_cast<const float2 *const *>(Aarray);
+        g.B = reinterpret_cast<const float2 *const *>(Barray);
+        g.C = reinterpret_cast<float2 *const *>(Carray);
+        g.lda = lda; g.ldb = ldb; g.ldc = ldc;
+        g.alpha = al; g.beta = be; g.beta_zero = beta_zero;
+        dim3 grid((unsigned)mdt::cdiv(m, 16), (unsigned)mdt::cdiv(n, 16), (unsigned)batchCount);
+        mdt::cgemm_batched_kernel<<<grid, dim3(16, 16), 0, handle->stream>>>(g);
+        st = mdt::launch_status("cgemm_batched_kernel");
+    }
+    return st == MDT_SUCCESS ? CUBLAS_STATUS_SUCCESS : CUBLAS_STATUS_EXECUTION_FAILED;
+}
+
+}  // extern "C"
