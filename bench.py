@@ -287,24 +287,30 @@ def run_ours(args, cfg):
                                "SM clock" % nsm}
 
     # ---- e2e through the host-buffer C-ABI entry (pinned host memory)
-    h_iq = torch.empty(total_sp * sb, dtype=torch.int8, pin_memory=True)
-    h_iq.copy_(iq)
-    h_vis = torch.empty(nint * nch * ne * ne * 2, dtype=torch.float32, pin_memory=True)
-    plan.execute_host(h_iq, nint, h_vis)  # warm-up: staging buffers
-    e2e_steps = max(1, min(args.steps, 5))
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        plan.execute_host(h_iq, nint, h_vis)
-    barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if dist is not None:
-        tt = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    # host result agrees with the device-resident run of the same stream
-    ok = torch.equal(h_vis.view(torch.int32).view(-1).cpu(),
-                     vis.view(torch.float32).view(torch.int32).view(-1).cpu())
+    e2e = None
+    if not args.no_e2e:
+        h_iq = torch.empty(total_sp * sb, dtype=torch.int8, pin_memory=True)
+        h_iq.copy_(iq)
+        h_vis = torch.empty(nint * nch * ne * ne * 2, dtype=torch.float32, pin_memory=True)
+        plan.execute_host(h_iq, nint, h_vis)  # warm-up: staging buffers
+        e2e_steps = max(1, min(args.steps, 5))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            plan.execute_host(h_iq, nint, h_vis)
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        if dist is not None:
+            tt = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_s = float(tt.item())
+        # host result agrees with the device-resident run of the same stream
+        ok = torch.equal(h_vis.view(torch.int32).view(-1).cpu(),
+                         vis.view(torch.float32).view(torch.int32).view(-1).cpu())
+        e2e = {"value": samples / e2e_s, "unit": "antenna-samples/s",
+               "h2d_bytes_per_step": int(h_iq.numel()),
+               "d2h_bytes_per_step": int(h_vis.numel() * 4),
+               "api": "mdt_fx_execute_host", "matches_device_run": bool(ok)}
 
     line = None
     if rank == 0:
@@ -321,10 +327,7 @@ def run_ours(args, cfg):
             "config": {"workload": cfg.name, "nelements": ne, "nchannels": nch, "ntaps": ntaps,
                        "nspectra": nsp, "integrations": nint, "path": "fused FP32 plan API",
                        "l2": "inputs (%.1f GB) larger than L2, no flush" % (iq.numel() / 1e9)},
-            "e2e": {"value": samples / e2e_s, "unit": "antenna-samples/s",
-                    "h2d_bytes_per_step": int(h_iq.numel()),
-                    "d2h_bytes_per_step": int(h_vis.numel() * 4),
-                    "api": "mdt_fx_execute_host", "matches_device_run": bool(ok)},
+            "e2e": e2e,
             "gpu_launches": 2 * nint * args.steps,
             "roofline": roof,
             "kernels": kernels,
@@ -348,11 +351,17 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0,
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e run")
+    ap.add_argument("--integrations", type=int, default=None,
+                    help="override the number of integrations per step (small profiling "
+                         "cases)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     mdt = load_pkg()
     cfg = mdt.configs.CONFIGS[args.config]
+    if args.integrations:
+        cfg = mdt.configs.small(cfg, nint=args.integrations)
     if args.impl == "reference":
         run_reference(args, cfg)
     else:

@@ -137,7 +137,9 @@ MDT_API mdt_status mdt_xengine_f32(int ne, int nch, int nsp, const void *X, long
 /* Fused F-engine, FP32: int8 I/Q -> PFB (fmaf in the reference's tap order)
  * -> FFT -> channel-major complex64 X[(c*Nsp + s)*NE + e].
  * `iq` holds Nsp + Ntaps - 1 spectra.  Bit-identical to PpS_Batch ->
- * cufftExecC2C (this library) -> ReorderFOutput on the same samples. */
+ * cufftExecC2C (this library) -> ReorderFOutput on the same samples.
+ * `iq` and `window` must be 16-byte aligned (as are the sample buffers passed
+ * to the plan entry points below). */
 MDT_API mdt_status mdt_fengine_f32(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
                                    const float *window, void *X, cudaStream_t stream);
 
@@ -156,7 +158,10 @@ MDT_API mdt_status mdt_synth_iq(uint64_t seed, int ne, int nch, long s0, long ns
  * ---------------------------------------------------------------------- */
 
 typedef enum {
-    MDT_PREC_FP32 = 0 /* complex64 F-output, FP32 SIMT X-engine (<=1e-5 vs FP64) */
+    MDT_PREC_FP32 = 0, /* complex64 F-output, FP32 SIMT X-engine (<=1e-5 vs FP64) */
+    MDT_PREC_FP16 = 1, /* f16 F-output (power-of-two scaled), tcgen05 X-engine, FP32
+                          accumulate (<=1e-3 vs FP64); Nch <= 4096 */
+    MDT_PREC_BF16 = 2  /* as FP16 with bf16 operands */
 } mdt_precision;
 
 typedef struct {
@@ -177,6 +182,18 @@ MDT_API mdt_status mdt_fx_destroy(mdt_fx_plan plan);
 MDT_API mdt_status mdt_fx_set_stream(mdt_fx_plan plan, cudaStream_t stream);
 /* Copies Ntaps*Nch floats from a device pointer into the plan. */
 MDT_API mdt_status mdt_fx_set_window(mdt_fx_plan plan, const float *window);
+/* FP64 cross-integration accumulation: when `acc` (device, complex128
+ * [Nch][NE*NE], 16-byte aligned, zeroed by the caller) is set, every
+ * integration's visibilities are also added into it; NULL disables. */
+MDT_API mdt_status mdt_fx_set_accumulator(mdt_fx_plan plan, void *acc);
+/* The power-of-two scale applied to the F-engine output before rounding to
+ * f16/bf16 (chosen from the window at mdt_fx_set_window; 1 for FP32); the
+ * visibilities are divided by scale^2. */
+MDT_API mdt_status mdt_fx_get_scale(mdt_fx_plan plan, float *scale);
+/* Waits for the plan's stream and reports MDT_ERR_TIMEOUT if a bounded
+ * device-side wait of the tensor-core X-engine gave up since the last check
+ * (the flag is then cleared). */
+MDT_API mdt_status mdt_fx_check(mdt_fx_plan plan);
 /* Bytes of device memory the plan holds. */
 MDT_API mdt_status mdt_fx_workspace_bytes(mdt_fx_plan plan, size_t *bytes);
 

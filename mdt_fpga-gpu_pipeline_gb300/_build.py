@@ -40,8 +40,8 @@ def _deps():
     return dep
 
 
-def _compile(src, extra):
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+def _compile(src, extra, build_dir):
+    obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + ["-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -56,27 +56,30 @@ def up_to_date():
     return all(os.path.getmtime(p) <= t for p in _deps())
 
 
-def build(force=False, verbose=False, extra=None):
-    """Compile and link libmdtfx.so; returns its path."""
-    if not force and up_to_date():
+def build(force=False, verbose=False, extra=None, out=None):
+    """Compile and link libmdtfx.so (or `out`); returns its path.  `extra`
+    holds additional nvcc flags (e.g. -D tuning macros) for every unit."""
+    lib_path = out or LIB
+    if not force and out is None and not extra and up_to_date():
         return LIB
-    os.makedirs(BUILD, exist_ok=True)
+    build_dir = BUILD if out is None else out + ".objs"
+    os.makedirs(build_dir, exist_ok=True)
     extra = list(extra or [])
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        results = list(ex.map(lambda s: _compile(s, extra), srcs))
+        results = list(ex.map(lambda s: _compile(s, extra, build_dir), srcs))
     if verbose:
         for obj, err in results:
             if err.strip():
                 print(err)
     objs = [o for o, _ in results]
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib_path + ".tmp%d" % os.getpid()
     cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -17,7 +17,7 @@ CUFFT_FORWARD = -1
 CUFFT_INVERSE = 1
 CUFFT_C2C = 0x29
 CUBLAS_OP_N, CUBLAS_OP_T, CUBLAS_OP_C = 0, 1, 2
-MDT_PREC_FP32 = 0
+MDT_PREC_FP32, MDT_PREC_FP16, MDT_PREC_BF16 = 0, 1, 2
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -65,6 +65,9 @@ def _declare(L):
         "mdt_fx_stream_reset": ([_P], _I),
         "mdt_fx_stream_push": ([_P, _P, _P], _I),
         "mdt_fx_execute_host": ([_P, _P, _I, _P], _I),
+        "mdt_fx_set_accumulator": ([_P, _P], _I),
+        "mdt_fx_get_scale": ([_P, ctypes.POINTER(ctypes.c_float)], _I),
+        "mdt_fx_check": ([_P], _I),
         "mdt_fx_set_timing": ([_P, _I], _I),
         "mdt_fx_get_timing": ([_P, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)], _I),
@@ -273,6 +276,19 @@ class FxPlan:
 
     def set_window(self, window):
         check(lib().mdt_fx_set_window(self._h, ptr(window)), "mdt_fx_set_window")
+
+    def set_accumulator(self, acc):
+        """FP64 cross-integration accumulator (complex128 CUDA tensor) or None."""
+        check(lib().mdt_fx_set_accumulator(self._h, ptr(acc)), "mdt_fx_set_accumulator")
+
+    def scale(self):
+        v = ctypes.c_float(0)
+        check(lib().mdt_fx_get_scale(self._h, ctypes.byref(v)), "mdt_fx_get_scale")
+        return v.value
+
+    def check(self):
+        """Synchronise and raise on a device-side wait timeout."""
+        check(lib().mdt_fx_check(self._h), "mdt_fx_check")
 
     def workspace_bytes(self):
         v = ctypes.c_size_t(0)

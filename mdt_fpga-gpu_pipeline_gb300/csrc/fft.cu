@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(RowsCfg<N>::THREADS)
     auto store = [&](int i, float2 v) {
         if (valid) dst[i] = inverse ? cconj(v) : v;
     };
-    fft::transform_row<N, C::TPR>(sre, sim, t, tw, load, store);
+    fft::transform_row<N, C::TPR, true, true>(sre, sim, t, tw, load, store);
 }
 
 template <int N>

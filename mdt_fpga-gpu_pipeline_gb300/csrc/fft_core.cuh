@@ -20,6 +20,12 @@
 #pragma once
 #include "mdt_common.cuh"
 
+// Radix-8 twiddles: 0 = seven table loads per butterfly; 1 = three loads and
+// four complex products (fewer load instructions, a few ulp more rounding).
+#ifndef MDT_FFT_TW_PRODUCTS
+#define MDT_FFT_TW_PRODUCTS 1
+#endif
+
 namespace mdt {
 namespace fft {
 
@@ -97,9 +103,12 @@ __device__ __forceinline__ void dft<8>(float2 *v)
 
 // One Stockham pass over one row.  `t` is the thread's index within the row
 // (0..TPR-1); every thread of the block must call every pass (barriers).
-// FIRST: inputs come from load(i); otherwise from shared memory.
-// LAST : outputs go to store(i, v); otherwise to shared memory.
-template <int N, int TPR, int P, bool FIRST, bool LAST, class Load, class Store>
+// LOADFN (pass 0 only): inputs come from load(i) instead of shared memory,
+//   so no barrier is needed before the pass writes shared memory.
+// STOREFN (last pass only): outputs go to store(i, v) instead of shared memory.
+// Padded indices are formed from the pass's compile-time strides where the
+// strides are multiples of 8 (pad(x + 8k) = pad(x) + 9k).
+template <int N, int TPR, int P, bool LOADFN, bool STOREFN, class Load, class Store>
 __device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
                                               const float2 *__restrict__ tw, Load &load,
                                               Store &store)
@@ -116,22 +125,41 @@ __device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
 #pragma unroll
             for (int m = 0; m < R; m++) {
                 const int idx = b + m * NB;
-                if constexpr (FIRST) {
+                if constexpr (LOADFN) {
                     v[k][m] = load(idx);
                 } else {
-                    v[k][m] = make_float2(sre[pad(idx)], sim[pad(idx)]);
+                    const int pi = (NB % 8 == 0) ? pad(b) + m * pad(NB) : pad(idx);
+                    v[k][m] = make_float2(sre[pi], sim[pi]);
                 }
             }
             if constexpr (NS > 1) {
                 const int jm = b & (NS - 1);
+                constexpr int TS = N / (NS * R);
+#if MDT_FFT_TW_PRODUCTS
+                // radix 8: w, w^2, w^4 from the table, the other powers as products
+                if constexpr (R == 8) {
+                    const float2 w1 = __ldg(&tw[jm * TS]), w2 = __ldg(&tw[2 * jm * TS]),
+                                 w4 = __ldg(&tw[4 * jm * TS]);
+                    const float2 w3 = cmul(w1, w2);
+                    v[k][1] = cmul(v[k][1], w1);
+                    v[k][2] = cmul(v[k][2], w2);
+                    v[k][3] = cmul(v[k][3], w3);
+                    v[k][4] = cmul(v[k][4], w4);
+                    v[k][5] = cmul(v[k][5], cmul(w1, w4));
+                    v[k][6] = cmul(v[k][6], cmul(w2, w4));
+                    v[k][7] = cmul(v[k][7], cmul(w3, w4));
+                } else
+#endif
+                {
 #pragma unroll
-                for (int m = 1; m < R; m++)
-                    v[k][m] = cmul(v[k][m], __ldg(&tw[m * jm * (N / (NS * R))]));
+                    for (int m = 1; m < R; m++)
+                        v[k][m] = cmul(v[k][m], __ldg(&tw[m * jm * TS]));
+                }
             }
             dft<R>(v[k]);
         }
     }
-    if constexpr (!FIRST) __syncthreads();  // every read of this pass precedes any write
+    if constexpr (!LOADFN) __syncthreads();  // every read of this pass precedes any write
 #pragma unroll
     for (int k = 0; k < NBT; k++) {
         const int b = t + k * TPR;
@@ -140,36 +168,42 @@ __device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
 #pragma unroll
             for (int m = 0; m < R; m++) {
                 const int o = base + m * NS;
-                if constexpr (LAST) {
+                if constexpr (STOREFN) {
                     store(o, v[k][m]);
                 } else {
-                    sre[pad(o)] = v[k][m].x;
-                    sim[pad(o)] = v[k][m].y;
+                    const int po = (NS % 8 == 0) ? pad(base) + m * pad(NS) : pad(o);
+                    sre[po] = v[k][m].x;
+                    sim[po] = v[k][m].y;
                 }
             }
         }
     }
-    if constexpr (!LAST) __syncthreads();  // writes visible to the next pass
+    if constexpr (!STOREFN) __syncthreads();  // writes visible to the next pass
 }
 
-template <int N, int TPR, int P, class Load, class Store>
+template <int N, int TPR, int P, bool LOADFN, bool STOREFN, class Load, class Store>
 __device__ __forceinline__ void run_passes(float *sre, float *sim, int t,
                                            const float2 *__restrict__ tw, Load &load,
                                            Store &store)
 {
     constexpr int NP = Shape<N>::NPASS;
-    stockham_pass<N, TPR, P, P == 0, P == NP - 1>(sre, sim, t, tw, load, store);
-    if constexpr (P + 1 < NP) run_passes<N, TPR, P + 1>(sre, sim, t, tw, load, store);
+    stockham_pass<N, TPR, P, LOADFN && P == 0, STOREFN && P == NP - 1>(sre, sim, t, tw, load,
+                                                                       store);
+    if constexpr (P + 1 < NP)
+        run_passes<N, TPR, P + 1, LOADFN, STOREFN>(sre, sim, t, tw, load, store);
 }
 
-// Transforms one row: first-pass inputs from load(i), natural-order outputs
-// to store(i, v).  sre/sim: this row's shared arrays of Shape<N>::PADN floats.
-template <int N, int TPR, class Load, class Store>
+// Transforms one row: first-pass inputs from load(i) (LOADFN) or from the
+// row's shared arrays in natural order (then the caller must have written
+// them and synchronised), natural-order outputs to store(i, v) (STOREFN) or
+// left in the shared arrays.  sre/sim: the row's arrays of Shape<N>::PADN
+// floats, element i at pad(i).
+template <int N, int TPR, bool LOADFN, bool STOREFN, class Load, class Store>
 __device__ __forceinline__ void transform_row(float *sre, float *sim, int t,
                                               const float2 *__restrict__ tw, Load &load,
                                               Store &store)
 {
-    run_passes<N, TPR, 0>(sre, sim, t, tw, load, store);
+    run_passes<N, TPR, 0, LOADFN, STOREFN>(sre, sim, t, tw, load, store);
 }
 
 }  // namespace fft

@@ -4,6 +4,8 @@
 // (MDT_OneStation_client.cu:1071-1152: PpS_Batch -> cufftExecC2C ->
 // ReorderFOutput -> cublasCgemmBatched, then the rank-3 history shift at
 // :1170) as two kernels per integration on one stream.
+#include <algorithm>
+#include <cmath>
 #include <new>
 #include <vector>
 
@@ -18,6 +20,26 @@ mdt_status xengine_herm_f32(int ne, long nbatch, int nsp, const float2 *X,
                             float2 *const *Vptrs, long ldv, long vstride, float2 alpha,
                             float2 beta, bool beta_zero, cudaStream_t stream);
 const float2 *fft_twiddles(int n, mdt_status *st);
+mdt_status fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
+                       const int8_t *iq, const float *win, void *X16, int nep, int nkc,
+                       int ab_fmt, float scale, cudaStream_t stream);
+mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, float scale,
+                      float2 *V, double2 *Vacc, int *err, cudaStream_t stream);
+int x16_padded_rows(int ne);
+int x16_chunks(int nsp);
+
+// Vacc[i] += V[i] (complex64 -> complex128), the cross-integration sum of the
+// FP32 path.
+__global__ void accumulate_f64_kernel(const float2 *__restrict__ V, double2 *__restrict__ acc,
+                                      long n)
+{
+    for (long i = threadIdx.x + (long)blockIdx.x * blockDim.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        float2 v = V[i];
+        double2 a = acc[i];
+        acc[i] = make_double2(a.x + (double)v.x, a.y + (double)v.y);
+    }
+}
 }  // namespace mdt
 
 struct mdt_fx_plan_s {
@@ -25,7 +47,12 @@ struct mdt_fx_plan_s {
     cudaStream_t stream = 0;
     float *window = nullptr;
     bool window_set = false;
-    float2 *X = nullptr;       // F-engine output, one integration
+    float2 *X = nullptr;       // F-engine output, one integration (FP32 path)
+    void *X16 = nullptr;       // F-engine output in the tensor-core operand layout
+    int nep = 0, nkc = 0;      // X16 padded rows and K-chunks
+    float scale = 1.0f;        // power-of-two F-output scale of the f16/bf16 path
+    int *err = nullptr;        // device flag set by a timed-out wait
+    double2 *acc = nullptr;    // optional FP64 cross-integration accumulator
     int8_t *hist[2] = {nullptr, nullptr};  // PFB history (double-buffered)
     int cur = 0;
     bool streaming = false;
@@ -51,6 +78,8 @@ void release(mdt_fx_plan p)
     if (!p) return;
     cudaFree(p->window);
     cudaFree(p->X);
+    cudaFree(p->X16);
+    cudaFree(p->err);
     cudaFree(p->hist[0]);
     cudaFree(p->hist[1]);
     for (int i = 0; i < 2; i++) {
@@ -88,16 +117,34 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
         if (!t0 || !t1 || !t2) return MDT_ERR_ALLOC;
         cudaEventRecord(t0, p->stream);
     }
-    mdt_status st = mdt::fengine_f32(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist,
-                                     iq, p->window, p->X, p->stream);
-    if (st != MDT_SUCCESS) return st;
-    if (t1) cudaEventRecord(t1, p->stream);
-    // X[c][s][e]: channel c operand is NE x Nsp column-major, ld = NE
-    st = mdt::xengine_herm_f32(d.nelements, d.nchannels, d.nspectra, p->X, nullptr, d.nelements,
-                               (long)d.nspectra * d.nelements, (float2 *)vis, nullptr,
-                               d.nelements, (long)d.nelements * d.nelements,
-                               make_float2(1.0f / d.nspectra, 0.f), make_float2(0.f, 0.f), true,
-                               p->stream);
+    mdt_status st;
+    if (d.precision == MDT_PREC_FP32) {
+        st = mdt::fengine_f32(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                              p->window, p->X, p->stream);
+        if (st != MDT_SUCCESS) return st;
+        if (t1) cudaEventRecord(t1, p->stream);
+        // X[c][s][e]: channel c operand is NE x Nsp column-major, ld = NE
+        st = mdt::xengine_herm_f32(d.nelements, d.nchannels, d.nspectra, p->X, nullptr,
+                                   d.nelements, (long)d.nspectra * d.nelements, (float2 *)vis,
+                                   nullptr, d.nelements, (long)d.nelements * d.nelements,
+                                   make_float2(1.0f / d.nspectra, 0.f), make_float2(0.f, 0.f),
+                                   true, p->stream);
+        if (st == MDT_SUCCESS && p->acc) {
+            long n = (long)d.nchannels * d.nelements * d.nelements;
+            mdt::accumulate_f64_kernel<<<(unsigned)std::min<long>(mdt::cdiv(n, 256),
+                                                                  (long)mdt::sm_count() * 16),
+                                         256, 0, p->stream>>>((const float2 *)vis, p->acc, n);
+            st = mdt::launch_status("accumulate_f64_kernel");
+        }
+    } else {
+        const int fmt = (d.precision == MDT_PREC_BF16) ? 1 : 0;
+        st = mdt::fengine_x16(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                              p->window, p->X16, p->nep, p->nkc, fmt, p->scale, p->stream);
+        if (st != MDT_SUCCESS) return st;
+        if (t1) cudaEventRecord(t1, p->stream);
+        st = mdt::xengine_tc(d.nelements, d.nchannels, d.nspectra, p->X16, fmt, p->scale,
+                             (float2 *)vis, p->acc, p->err, p->stream);
+    }
     if (st == MDT_SUCCESS && t2) cudaEventRecord(t2, p->stream);
     return st;
 }
@@ -113,8 +160,13 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
     mdt_status st = mdt::check_dims(desc->nelements, desc->nchannels, desc->ntaps,
                                     desc->nspectra);
     if (st != MDT_SUCCESS) return st;
-    if (desc->precision != MDT_PREC_FP32) {
+    if (desc->precision != MDT_PREC_FP32 && desc->precision != MDT_PREC_FP16 &&
+        desc->precision != MDT_PREC_BF16) {
         mdt::set_error("fx_create: precision not supported by this build");
+        return MDT_ERR_NOT_SUPPORTED;
+    }
+    if (desc->precision != MDT_PREC_FP32 && desc->nchannels > 4096) {
+        mdt::set_error("fx_create: the f16/bf16 path supports Nch <= 4096");
         return MDT_ERR_NOT_SUPPORTED;
     }
     mdt_fx_plan p = new (std::nothrow) mdt_fx_plan_s;
@@ -122,10 +174,22 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
     p->d = *desc;
     const mdt_fx_desc &d = p->d;
     size_t wbytes = sizeof(float) * (size_t)d.ntaps * d.nchannels;
-    size_t xbytes = sizeof(float2) * (size_t)d.nspectra * d.nelements * d.nchannels;
+    size_t xbytes = 0;
     size_t hbytes = spectrum_bytes(d) * (size_t)(d.ntaps - 1);
     cudaError_t e = cudaMalloc(&p->window, wbytes);
-    if (e == cudaSuccess) e = cudaMalloc(&p->X, xbytes);
+    if (d.precision == MDT_PREC_FP32) {
+        xbytes = sizeof(float2) * (size_t)d.nspectra * d.nelements * d.nchannels;
+        if (e == cudaSuccess) e = cudaMalloc(&p->X, xbytes);
+    } else {
+        p->nep = mdt::x16_padded_rows(d.nelements);
+        p->nkc = mdt::x16_chunks(d.nspectra);
+        xbytes = (size_t)d.nchannels * p->nkc * p->nep * 128;
+        if (e == cudaSuccess) e = cudaMalloc(&p->X16, xbytes);
+        // padding rows (elements NE..NEp-1) are never written: zero them once
+        if (e == cudaSuccess) e = cudaMemset(p->X16, 0, xbytes);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&p->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&p->hist[0], hbytes);
     if (e == cudaSuccess) e = cudaMalloc(&p->hist[1], hbytes);
     if (e != cudaSuccess) {
@@ -159,12 +223,60 @@ MDT_API mdt_status mdt_fx_set_stream(mdt_fx_plan plan, cudaStream_t stream)
 MDT_API mdt_status mdt_fx_set_window(mdt_fx_plan plan, const float *window)
 {
     if (!plan || !window) return mdt::invalid("fx_set_window: null argument");
-    size_t wbytes = sizeof(float) * (size_t)plan->d.ntaps * plan->d.nchannels;
-    mdt_status st = mdt::cuda_status(
-        cudaMemcpyAsync(plan->window, window, wbytes, cudaMemcpyDeviceToDevice, plan->stream),
-        "fx_set_window");
-    if (st == MDT_SUCCESS) plan->window_set = true;
+    size_t n = (size_t)plan->d.ntaps * plan->d.nchannels;
+    mdt_status st = mdt::cuda_status(cudaMemcpyAsync(plan->window, window, sizeof(float) * n,
+                                                     cudaMemcpyDeviceToDevice, plan->stream),
+                                     "fx_set_window");
+    if (st != MDT_SUCCESS) return st;
+    if (plan->d.precision != MDT_PREC_FP32) {
+        // F-output bound for int8 samples: |X| <= 127 sqrt(2) sum |W|; the
+        // f16 scale is the power of two that keeps that bound under 60000.
+        std::vector<float> h(n);
+        st = mdt::cuda_status(cudaMemcpy(h.data(), plan->window, sizeof(float) * n,
+                                         cudaMemcpyDeviceToHost),
+                              "fx_set_window: window bound");
+        if (st != MDT_SUCCESS) return st;
+        double sum = 0;
+        for (float w : h) sum += fabs((double)w);
+        double bound = 127.0 * 1.4142135623730951 * sum;
+        int ex = 0;
+        while (bound * std::ldexp(1.0, -ex) > 60000.0 && ex < 60) ex++;
+        plan->scale = (float)std::ldexp(1.0, -ex);
+    }
+    plan->window_set = true;
     return st;
+}
+
+MDT_API mdt_status mdt_fx_set_accumulator(mdt_fx_plan plan, void *acc)
+{
+    if (!plan) return mdt::invalid("fx_set_accumulator: null plan");
+    if (((uintptr_t)acc & 15) != 0) return mdt::invalid("fx_set_accumulator: misaligned buffer");
+    plan->acc = (double2 *)acc;
+    return MDT_SUCCESS;
+}
+
+MDT_API mdt_status mdt_fx_get_scale(mdt_fx_plan plan, float *scale)
+{
+    if (!plan || !scale) return mdt::invalid("fx_get_scale: null argument");
+    *scale = plan->scale;
+    return MDT_SUCCESS;
+}
+
+MDT_API mdt_status mdt_fx_check(mdt_fx_plan plan)
+{
+    if (!plan) return mdt::invalid("fx_check: null plan");
+    mdt_status st = mdt::cuda_status(cudaStreamSynchronize(plan->stream), "fx_check");
+    if (st != MDT_SUCCESS) return st;
+    int flag = 0;
+    st = mdt::cuda_status(cudaMemcpy(&flag, plan->err, sizeof(int), cudaMemcpyDeviceToHost),
+                          "fx_check");
+    if (st != MDT_SUCCESS) return st;
+    if (flag) {
+        cudaMemset(plan->err, 0, sizeof(int));
+        mdt::set_error("fx_check: a device-side wait timed out");
+        return MDT_ERR_TIMEOUT;
+    }
+    return MDT_SUCCESS;
 }
 
 MDT_API mdt_status mdt_fx_workspace_bytes(mdt_fx_plan plan, size_t *bytes)

@@ -1,0 +1,180 @@
+// tc_ptx.cuh -- inline-PTX wrappers for the Blackwell (sm_100a family,
+// here sm_103a) asynchronous machinery used by the tensor-core X-engine:
+// mbarriers, bulk (TMA) global->shared copies, tensor memory allocation,
+// tcgen05.mma / commit / ld, and the shared-memory matrix descriptor.
+#pragma once
+#include <stdint.h>
+
+namespace mdt {
+namespace tc {
+
+// Every wait on an mbarrier gives up after this many SM clock cycles
+// (~1 s at 2 GHz) and reports a timeout instead of spinning forever.
+constexpr long long kWaitCycles = 2000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+
+// Bounded wait that sleeps between polls (for threads that wait a long time
+// while others work, e.g. an epilogue waiting for the whole main loop).
+__device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) return false;
+        __nanosleep(256);
+    }
+    return true;
+}
+
+// Bulk copy (TMA, no tensor map) of `bytes` (multiple of 16, both addresses
+// 16-byte aligned) from global to this CTA's shared memory, completing
+// transaction bytes on mbarrier `bar`.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
+                                         uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+// ---- tensor memory (TMEM); alloc/dealloc/relinquish are warp-collective
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish()
+{
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_before_sync()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (f16 or bf16 inputs, f32 accumulate).
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive once on `bar` when all previously issued tcgen05.mma of this thread
+// have completed.
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     bar)
+                 : "memory");
+}
+
+// 16 consecutive 32-bit columns of this thread's TMEM lane (warp-collective;
+// the warp's lane quarter is encoded in taddr bits 31:16).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait()
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor for a K-major operand in the 128-byte
+// swizzled canonical layout: rows of 128 bytes, 8-row (1024-byte) swizzle
+// atoms, atoms 1024 bytes apart (stride byte offset), descriptor version 1,
+// swizzle mode 2 (128B).  The leading byte offset is unused for this layout.
+// Advancing K by 16 bf16/f16 elements inside the 128-byte row adds 32 bytes
+// to the start address (2 in the >>4 field).
+__device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t smem_addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((smem_addr & 0x3FFFF) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                        // leading byte offset (unused) = 16 B
+    d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset = 1024 B
+    d |= (uint64_t)1 << 46;                        // descriptor version
+    d |= (uint64_t)2 << 61;                        // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = f32, A/B = f16 (fmt 0) or bf16
+// (fmt 1), both K-major, M = 128, N (multiple of 16, <= 256), optional
+// negation of A.
+__host__ __device__ constexpr uint32_t idesc_f16(int n, int ab_fmt, int negate_a)
+{
+    return (1u << 4)                          // D format: f32
+           | ((uint32_t)ab_fmt << 7)          // A format
+           | ((uint32_t)ab_fmt << 10)         // B format
+           | ((uint32_t)negate_a << 13)       // negate A
+           | ((uint32_t)(n >> 3) << 17)       // N >> 3
+           | ((uint32_t)(128 >> 4) << 24);    // M >> 4
+}
+
+}  // namespace tc
+}  // namespace mdt

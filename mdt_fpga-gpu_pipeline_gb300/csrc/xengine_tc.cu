@@ -1,0 +1,253 @@
+// xengine_tc.cu -- Hermitian X-engine on the 5th-generation tensor cores
+// (tcgen05.mma kind::f16, accumulators in tensor memory), replacing
+// cublasCgemmBatched(OP_N, OP_C, A == B) (reference
+// MDT_OneStation_client.cu:1128) for the reduced-precision path.
+//
+// Operand layout ("X16"), written by the f16/bf16 F-engine: for channel c and
+// K-chunk kc of 32 spectra, a block of NEp rows (elements, NE rounded up to
+// 16, zero rows beyond NE) of 128 bytes:
+//     row e = [ re(s0..s0+31) | im(s0..s0+31) ]   (32 + 32 f16/bf16 values)
+// with the 128-byte swizzle applied inside each 8-row atom (16-byte chunk j
+// of row e stored at chunk j ^ (e & 7)), i.e. exactly the K-major SW128
+// canonical layout, so any run of rows is one contiguous bulk copy that
+// lands in shared memory ready for the tensor core.  Spectra beyond Nsp in
+// the last chunk are zero.
+//
+// Per 128-byte row (32 spectra) the complex product V = X X^H is eight real
+// K=16 MMAs on two accumulators (k-steps 0,1 = re, 2,3 = im):
+//     Re V += A0 B0 + A1 B1 + A2 B2 + A3 B3
+//     Im V += A2 B0 + A3 B1 - A0 B2 - A1 B3        (negate-A bit)
+// A block owns one (channel, row tile of 128 elements, column chunk of up to
+// 256 elements) of the lower triangle: only tiles on or below the diagonal
+// are computed; the epilogue writes the lower triangle and its conjugate
+// mirror (full square, column-major, the cuBLAS C layout) and can add the
+// result into an FP64 cross-integration accumulator.
+//
+// Warp roles (192 threads): warp 0 lane 0 issues bulk copies into a 4-stage
+// shared-memory ring; warp 1 allocates tensor memory and its lane 0 issues
+// the MMAs and commits; warps 2-5 read the accumulators (one TMEM lane
+// quarter each) and write visibilities.  Every mbarrier wait is bounded; a
+// timeout sets the error flag and the block finishes without further work.
+#include "mdt_common.cuh"
+#include "tc_ptx.cuh"
+
+namespace mdt {
+
+constexpr int TC_STAGES = 4;
+constexpr int TC_BROWS = 256;  // max column-chunk rows (N)
+constexpr int TC_AROWS = 128;  // row tile (M)
+constexpr int TC_THREADS = 192;
+constexpr int TC_MAX_TILES = 160;
+constexpr uint32_t TC_B_BYTES = TC_BROWS * 128;
+constexpr uint32_t TC_A_BYTES = TC_AROWS * 128;
+constexpr uint32_t TC_STAGE_BYTES = TC_B_BYTES + TC_A_BYTES;
+constexpr size_t TC_SMEM = 1024 /*align slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES + 256;
+
+struct TcTile {
+    int16_t r0, q0, n, a_sep;  // row-tile start, column-chunk start, chunk width, A loaded apart
+};
+
+struct TcArgs {
+    const uint8_t *X;   // X16 operand base
+    long chunk_bytes;   // NEp * 128
+    long chan_bytes;    // nkc * NEp * 128
+    int ne, nep, nkc;
+    int ntiles;
+    int ab_fmt;         // 0 = f16, 1 = bf16
+    float alpha;        // applied to the accumulators (1/(Nsp * scale^2))
+    float2 *V;          // [nch][ne*ne] complex64, column-major per channel (may be null)
+    double2 *Vacc;      // [nch][ne*ne] complex128 accumulator (may be null)
+    int *err;           // set to 1 on a wait timeout
+    TcTile tiles[TC_MAX_TILES];
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_constant__ TcArgs a)
+{
+    extern __shared__ uint8_t smem_raw[];
+    // 1024-byte alignment for the swizzle atoms
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + (size_t)TC_STAGES * TC_STAGE_BYTES);
+    // bars[0..S) full, bars[S..2S) empty, bars[2S] done; then the TMEM address slot
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ch = blockIdx.x / a.ntiles;
+    const TcTile tile = a.tiles[blockIdx.x - ch * a.ntiles];
+    const int N = tile.n;
+    const uint32_t ncols = (2 * N <= 32) ? 32 : (2 * N <= 64) ? 64 : (2 * N <= 128) ? 128
+                                                                   : (2 * N <= 256) ? 256 : 512;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2 * TC_STAGES + 1; s++) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(tc::smem_u32(tmem_slot), ncols);
+        tc::tmem_relinquish();
+        tc::fence_before_sync();
+    }
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t d_re = tmem, d_im = tmem + (uint32_t)N;
+
+    const uint8_t *xc = a.X + (long)ch * a.chan_bytes;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- producer: bulk copies into the stage ring
+        const uint32_t bbytes = (uint32_t)N * 128;
+        const int arows = min(TC_AROWS, a.nep - tile.r0);
+        const uint32_t abytes = tile.a_sep ? (uint32_t)arows * 128 : 0;
+        for (int kc = 0; kc < a.nkc && ok; kc++) {
+            const int s = kc % TC_STAGES;
+            if (kc >= TC_STAGES) {
+                ok = tc::mbar_wait(tc::smem_u32(&bars[TC_STAGES + s]), ((kc / TC_STAGES) - 1) & 1);
+                if (!ok) break;
+            }
+            uint8_t *stage = smem + (size_t)s * TC_STAGE_BYTES;
+            const uint32_t full = tc::smem_u32(&bars[s]);
+            tc::mbar_expect_tx(full, bbytes + abytes);
+            const uint8_t *src = xc + (long)kc * a.chunk_bytes;
+            tc::bulk_g2s(tc::smem_u32(stage), src + (long)tile.q0 * 128, bbytes, full);
+            if (abytes)
+                tc::bulk_g2s(tc::smem_u32(stage + TC_B_BYTES), src + (long)tile.r0 * 128, abytes,
+                             full);
+        }
+        // drain: wait until the MMAs consumed every issued stage, so no copy
+        // is in flight when the block exits
+        if (ok) {
+            for (int kc = max(0, a.nkc - TC_STAGES); kc < a.nkc && ok; kc++)
+                ok = tc::mbar_wait(tc::smem_u32(&bars[TC_STAGES + (kc % TC_STAGES)]),
+                                   (kc / TC_STAGES) & 1);
+        }
+        if (!ok) atomicExch(a.err, 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer
+        const uint32_t id_pos = tc::idesc_f16(N, a.ab_fmt, 0);
+        const uint32_t id_neg = tc::idesc_f16(N, a.ab_fmt, 1);
+        for (int kc = 0; kc < a.nkc && ok; kc++) {
+            const int s = kc % TC_STAGES;
+            ok = tc::mbar_wait(tc::smem_u32(&bars[s]), (kc / TC_STAGES) & 1);
+            if (!ok) break;
+            tc::fence_after_sync();
+            const uint32_t sb = tc::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
+            const uint32_t sa = tile.a_sep ? sb + TC_B_BYTES : sb + (uint32_t)(tile.r0 - tile.q0) * 128;
+            const uint64_t bd = tc::sw128_kmajor_desc(sb);
+            const uint64_t ad = tc::sw128_kmajor_desc(sa);
+            const uint32_t first = (kc == 0);
+            // k-step j advances the start address by 32 bytes (+2 in the >>4 field)
+            tc::mma_f16(d_re, ad + 0, bd + 0, id_pos, !first);
+            tc::mma_f16(d_re, ad + 2, bd + 2, id_pos, 1);
+            tc::mma_f16(d_re, ad + 4, bd + 4, id_pos, 1);
+            tc::mma_f16(d_re, ad + 6, bd + 6, id_pos, 1);
+            tc::mma_f16(d_im, ad + 4, bd + 0, id_pos, !first);
+            tc::mma_f16(d_im, ad + 6, bd + 2, id_pos, 1);
+            tc::mma_f16(d_im, ad + 0, bd + 4, id_neg, 1);
+            tc::mma_f16(d_im, ad + 2, bd + 6, id_neg, 1);
+            tc::mma_commit(tc::smem_u32(&bars[TC_STAGES + s]));
+        }
+        tc::mma_commit(tc::smem_u32(&bars[2 * TC_STAGES]));
+        if (!ok) atomicExch(a.err, 1);
+    } else if (warp >= 2) {
+        // ---------------- epilogue: TMEM -> visibilities
+        ok = tc::mbar_wait_sleep(tc::smem_u32(&bars[2 * TC_STAGES]), 0);
+        tc::fence_after_sync();
+        const int quarter = warp & 3;
+        const int r = tile.r0 + quarter * 32 + lane;
+        const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+        float2 *Vc = a.V ? a.V + (long)ch * a.ne * a.ne : nullptr;
+        double2 *Ac = a.Vacc ? a.Vacc + (long)ch * a.ne * a.ne : nullptr;
+        for (int n0 = 0; n0 < N; n0 += 16) {
+            uint32_t vr[16], vi[16];
+            tc::tmem_ld16(d_re + lane_off + n0, vr);
+            tc::tmem_ld16(d_im + lane_off + n0, vi);
+            tc::tmem_ld_wait();
+            if (!ok || r >= a.ne) continue;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int q = tile.q0 + n0 + j;
+                if (q >= a.ne || q > r) continue;
+                const float re = __uint_as_float(vr[j]) * a.alpha;
+                const float im = (q == r) ? 0.0f : __uint_as_float(vi[j]) * a.alpha;
+                const long lo = (long)q * a.ne + r, up = (long)r * a.ne + q;
+                if (Vc) {
+                    Vc[lo] = make_float2(re, im);
+                    if (q != r) Vc[up] = make_float2(re, -im);
+                }
+                if (Ac) {
+                    double2 x = Ac[lo];
+                    Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
+                    if (q != r) {
+                        double2 y = Ac[up];
+                        Ac[up] = make_double2(y.x + (double)re, y.y - (double)im);
+                    }
+                }
+            }
+        }
+        if (!ok && lane == 0) atomicExch(a.err, 1);
+        tc::fence_before_sync();
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, ncols);
+    }
+}
+
+// Lower-triangle work list for NE elements: row tiles of 128, column chunks
+// of up to 256 from 0 to the end of the row tile's diagonal block.
+static int make_tiles(int ne, int nep, TcTile *tiles)
+{
+    int n = 0;
+    for (int r0 = 0; r0 < nep; r0 += TC_AROWS) {
+        const int cend = std::min(nep, r0 + TC_AROWS);
+        for (int q0 = 0; q0 < cend; q0 += TC_BROWS) {
+            if (n >= TC_MAX_TILES) return -1;
+            const int w = std::min(TC_BROWS, cend - q0);
+            TcTile t;
+            t.r0 = (int16_t)r0;
+            t.q0 = (int16_t)q0;
+            t.n = (int16_t)w;
+            // A inside the loaded B rows iff the chunk covers rows r0..r0+127
+            // (rows past NEp read stale shared memory and only feed
+            // accumulator rows that are never stored)
+            t.a_sep = (int16_t)(q0 + w <= r0 ? 1 : 0);
+            tiles[n++] = t;
+        }
+    }
+    return n;
+}
+
+int x16_padded_rows(int ne) { return (ne + 15) / 16 * 16; }
+int x16_chunks(int nsp) { return (nsp + 31) / 32; }
+
+mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, float scale,
+                      float2 *V, double2 *Vacc, int *err, cudaStream_t stream)
+{
+    if (!X16 || (!V && !Vacc) || !err) return invalid("xengine_tc: null pointer");
+    if (((uintptr_t)X16 & 15) != 0) return invalid("xengine_tc: X16 must be 16-byte aligned");
+    TcArgs a;
+    a.ne = ne;
+    a.nep = x16_padded_rows(ne);
+    a.nkc = x16_chunks(nsp);
+    a.chunk_bytes = (long)a.nep * 128;
+    a.chan_bytes = (long)a.nkc * a.chunk_bytes;
+    a.X = (const uint8_t *)X16;
+    a.ab_fmt = ab_fmt;
+    a.alpha = 1.0f / ((float)nsp * scale * scale);
+    a.V = V;
+    a.Vacc = Vacc;
+    a.err = err;
+    a.ntiles = make_tiles(ne, a.nep, a.tiles);
+    if (a.ntiles <= 0) return invalid("xengine_tc: too many tiles");
+    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "xengine_tc smem attribute");
+    long blocks = (long)nch * a.ntiles;
+    if (blocks > 0x7fffffffL) return invalid("xengine_tc: grid too large");
+    xengine_tc_kernel<<<(unsigned)blocks, TC_THREADS, TC_SMEM, stream>>>(a);
+    return launch_status("xengine_tc_kernel");
+}
+
+}  // namespace mdt
