@@ -184,6 +184,87 @@ def run_reference(args, cfg):
     print(json.dumps(line))
 
 
+def measure_plan(mdt, cfg, precision, dev, steps, warmup, seed_offset=0):
+    """Device-timed streamed FX over cfg.nint integrations with the plan API.
+    Returns (ms per step, F-engine ms per launch, X-engine ms per launch,
+    plan scale)."""
+    import torch
+    ne, nch, ntaps, nsp, nint = cfg.nelements, cfg.nchannels, cfg.ntaps, cfg.nspectra, cfg.nint
+    sb = ne * nch * 2
+    total_sp = nint * nsp + ntaps - 1
+
+    def t(a):
+        return None if a is None else torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    iq = torch.empty(total_sp * sb, dtype=torch.int8, device=dev)
+    ssig, sdel = cfg.sources()
+    mdt.synth_iq(cfg.seed + seed_offset, ne, nch, 0, total_sp, t(cfg.sigma_q8()), iq,
+                 tone_q16=t(cfg.tone_q16()), src_sigma_q8=t(ssig), src_delay=t(sdel))
+    win = torch.empty(nch * ntaps, dtype=torch.float32, device=dev)
+    mdt.window_hamming_sinc(nch, ntaps, win)
+    vis = torch.empty(nint, nch, ne, ne, dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    plan = mdt.FxPlan(ne, nch, ntaps, nsp, precision=precision, stream=stream)
+    plan.set_window(win)
+    first = (nsp + ntaps - 1) * sb
+
+    def step():
+        plan.stream_reset()
+        plan.stream_push(iq[:first], vis[0])
+        for j in range(1, nint):
+            lo = (j * nsp + ntaps - 1) * sb
+            plan.stream_push(iq[lo:lo + nsp * sb], vis[j])
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    plan.set_timing(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    f_ms, x_ms, count = plan.get_timing()
+    plan.check()
+    scale = plan.scale()
+    plan.close()
+    del iq, vis
+    torch.cuda.empty_cache()
+    return ms, f_ms / max(count, 1), x_ms / max(count, 1), scale
+
+
+def tensor_path_section(mdt, dev, steps):
+    """c3_array256 (NE=256, Nch=1024, Ntaps=8, Nsp=8192): the f16 tensor-core
+    path over the full 8 integrations and the plain FP32 path over one
+    integration, in antenna-samples/s, with the tensor X-engine's TFLOP/s."""
+    c3 = mdt.configs.C3
+    hbm, bf16, kind = peaks()
+    ms16, f16, x16, scale = measure_plan(mdt, c3, 1, dev, steps=steps, warmup=1)
+    c3_one = mdt.configs.small(c3, nint=1)
+    ms32, f32, x32, _ = measure_plan(mdt, c3_one, 0, dev, steps=1, warmup=1)
+    ne, nch, nsp, ntaps = c3.nelements, c3.nchannels, c3.nspectra, c3.ntaps
+    flops = 8.0 * ne * (ne + 1) / 2 * nsp * nch
+    v16 = c3.antenna_samples() / (ms16 * 1e-3)
+    v32 = c3_one.antenna_samples() / (ms32 * 1e-3)
+    x_tflops = flops / (x16 * 1e-3) / 1e12
+    f_bytes = (nsp + ntaps - 1) * ne * nch * 2 + nch * ((nsp + 31) // 32) * ((ne + 15) // 16 * 16) * 128
+    return {
+        "workload": c3.name, "precision": "f16 operands, fp32 accumulate (tcgen05 kind::f16)",
+        "value": v16, "unit": "antenna-samples/s", "ms_per_step": ms16,
+        "integrations": c3.nint, "fp32_path_value": v32, "speedup_vs_fp32_path": v16 / v32,
+        "xengine_tc": {"ms_per_launch": x16, "tflops": x_tflops, "peak": bf16,
+                       "frac": x_tflops / bf16, "peak_source": kind + " bf16_tflops (dense)",
+                       "algorithmic_flops": flops},
+        "fengine_x16": {"ms_per_launch": f16, "gbs": f_bytes / (f16 * 1e-3) / 1e9,
+                        "frac": f_bytes / (f16 * 1e-3) / 1e9 / hbm, "algorithmic_bytes": f_bytes},
+        "fp32_path": {"fengine_ms": f32, "xengine_ms": x32},
+        "f16_scale": scale,
+    }
+
+
 def run_ours(args, cfg):
     import torch
     mdt = load_pkg()
@@ -210,7 +291,8 @@ def run_ours(args, cfg):
     mdt.window_hamming_sinc(nch, ntaps, win)
     vis = torch.empty(nint, nch, ne, ne, dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
-    plan = mdt.FxPlan(ne, nch, ntaps, nsp, stream=stream)
+    prec = {"fp32": 0, "fp16": 1, "bf16": 2}[args.precision]
+    plan = mdt.FxPlan(ne, nch, ntaps, nsp, precision=prec, stream=stream)
     plan.set_window(win)
 
     first = (nsp + ntaps - 1) * sb
@@ -266,25 +348,33 @@ def run_ours(args, cfg):
     sm_mhz = clk.get("sm_mhz") or 1900.0
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = nsm * 128 * 2 * sm_mhz * 1e6 / 1e12  # FP32 FMA lanes at the sampled clock
+    if args.precision == "fp32":
+        fname, xname, xbound, xpeak = "fengine_f32", "xengine_herm_f32", "fp32", fp32_peak
+        xpeak_src = ("nominal FP32 FMA rate (%d SMs x 128 lanes x 2) at the sampled SM clock"
+                     % nsm)
+    else:
+        nep, nkc = (ne + 15) // 16 * 16, (nsp + 31) // 32
+        f_bytes = (nsp + ntaps - 1) * sb + nch * nkc * nep * 128 + ntaps * nch * 4
+        f_gbs = f_bytes / (f_launch_ms * 1e-3) / 1e9
+        x_bytes = nch * nkc * nep * 128 + nch * ne * ne * 8
+        x_gbs = x_bytes / (x_launch_ms * 1e-3) / 1e9
+        fname, xname, xbound, xpeak = "fengine_x16", "xengine_tc", "tensor", bf16
+        xpeak_src = peak_kind + " bf16_tflops (dense, burst)"
     kernels = {
-        "fengine_f32": {"ms_per_launch": f_launch_ms, "bound": "hbm", "achieved": f_gbs,
-                        "unit": "GB/s", "peak": hbm, "frac": f_gbs / hbm,
-                        "algorithmic_bytes": f_bytes},
-        "xengine_herm_f32": {"ms_per_launch": x_launch_ms, "bound": "fp32", "achieved": x_tflops,
-                             "unit": "TFLOP/s", "peak": fp32_peak, "frac": x_tflops / fp32_peak,
-                             "algorithmic_flops": x_flops, "hbm_gbs": x_gbs},
+        fname: {"ms_per_launch": f_launch_ms, "bound": "hbm", "achieved": f_gbs, "unit": "GB/s",
+                "peak": hbm, "frac": f_gbs / hbm, "algorithmic_bytes": f_bytes},
+        xname: {"ms_per_launch": x_launch_ms, "bound": xbound, "achieved": x_tflops,
+                "unit": "TFLOP/s", "peak": xpeak, "frac": x_tflops / xpeak,
+                "algorithmic_flops": x_flops, "hbm_gbs": x_gbs},
     }
     if f_launch_ms >= x_launch_ms:
-        name = "fengine_f32"
-        roof = {"kernel": name, "bound": "hbm", "achieved": f_gbs, "peak": hbm, "unit": "GB/s",
-                "frac": f_gbs / hbm, "traffic": NCU_TRAFFIC[name],
+        roof = {"kernel": fname, "bound": "hbm", "achieved": f_gbs, "peak": hbm, "unit": "GB/s",
+                "frac": f_gbs / hbm, "traffic": NCU_TRAFFIC.get(fname),
                 "peak_source": peak_kind + " hbm_gbs"}
     else:
-        name = "xengine_herm_f32"
-        roof = {"kernel": name, "bound": "fp32", "achieved": x_tflops, "peak": fp32_peak,
-                "unit": "TFLOP/s", "frac": x_tflops / fp32_peak, "traffic": NCU_TRAFFIC[name],
-                "peak_source": "nominal FP32 FMA rate (%d SMs x 128 lanes x 2) at the sampled "
-                               "SM clock" % nsm}
+        roof = {"kernel": xname, "bound": xbound, "achieved": x_tflops, "peak": xpeak,
+                "unit": "TFLOP/s", "frac": x_tflops / xpeak, "traffic": NCU_TRAFFIC.get(xname),
+                "peak_source": xpeak_src}
 
     # ---- e2e through the host-buffer C-ABI entry (pinned host memory)
     e2e = None
@@ -312,6 +402,10 @@ def run_ours(args, cfg):
                "d2h_bytes_per_step": int(h_vis.numel() * 4),
                "api": "mdt_fx_execute_host", "matches_device_run": bool(ok)}
 
+    tensor = None
+    if not args.no_tensor:
+        tensor = tensor_path_section(mdt, dev, steps=max(1, min(args.steps, 3)))
+
     line = None
     if rank == 0:
         cpu = None
@@ -322,10 +416,13 @@ def run_ours(args, cfg):
         line = {
             "metric": "F+X engine antenna-samples/s", "value": value, "unit": "antenna-samples/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "fp16": "f16 operands / f32 accumulate",
+                      "bf16": "bf16 operands / f32 accumulate"}[args.precision],
             "data": "synthetic (seeded integer int8 I/Q generator)",
             "config": {"workload": cfg.name, "nelements": ne, "nchannels": nch, "ntaps": ntaps,
-                       "nspectra": nsp, "integrations": nint, "path": "fused FP32 plan API",
+                       "nspectra": nsp, "integrations": nint,
+                       "path": "fused plan API, %s" % args.precision,
                        "l2": "inputs (%.1f GB) larger than L2, no flush" % (iq.numel() / 1e9)},
             "e2e": e2e,
             "gpu_launches": 2 * nint * args.steps,
@@ -333,6 +430,7 @@ def run_ours(args, cfg):
             "kernels": kernels,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "tensor_path": tensor,
         }
         print(json.dumps(line))
     plan.close()
@@ -352,6 +450,12 @@ def main():
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e run")
+    ap.add_argument("--no-tensor", action="store_true",
+                    help="skip the c3 tensor-core vs FP32 section")
+    ap.add_argument("--precision", choices=["fp32", "fp16", "bf16"], default="fp32",
+                    help="plan precision of the main measurement")
+    ap.add_argument("--nspectra", type=int, default=None,
+                    help="override spectra per integration (small profiling cases)")
     ap.add_argument("--integrations", type=int, default=None,
                     help="override the number of integrations per step (small profiling "
                          "cases)")
@@ -362,6 +466,8 @@ def main():
     cfg = mdt.configs.CONFIGS[args.config]
     if args.integrations:
         cfg = mdt.configs.small(cfg, nint=args.integrations)
+    if args.nspectra:
+        cfg = mdt.configs.small(cfg, nspectra=args.nspectra)
     if args.impl == "reference":
         run_reference(args, cfg)
     else:

@@ -143,6 +143,37 @@ MDT_API mdt_status mdt_xengine_f32(int ne, int nch, int nsp, const void *X, long
 MDT_API mdt_status mdt_fengine_f32(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
                                    const float *window, void *X, cudaStream_t stream);
 
+/* Fused F-engine, FP32, into the 8-spectrum blocked layout the plan's FP32
+ * path uses:  XB[c][s/8][e][s%8] complex64 (ceil(Nsp/8) blocks, spectra past
+ * Nsp zero) -- per channel one 64-byte run per (8 spectra, element).  Same
+ * values as mdt_fengine_f32 (bit-identical), Nch <= 2048. */
+MDT_API mdt_status mdt_fengine_c64b(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                    const float *window, void *XB, cudaStream_t stream);
+
+/* Fused F-engine for the tensor-core path: int8 I/Q -> PFB -> FFT -> output
+ * scaled by `scale` (a power of two keeps it exact) and rounded to f16
+ * (ab_fmt 0) or bf16 (ab_fmt 1) in the X16 operand layout:
+ *   X16[c][kc][e][128 bytes], kc = 32-spectrum chunk (ceil(Nsp/32) chunks),
+ *   e < NEp = NE rounded up to 16, row = [re(32 spectra) | im(32 spectra)],
+ *   16-byte chunk j of row e stored at chunk j ^ (e & 7) (the K-major
+ *   128-byte-swizzled layout the tensor cores read), spectra past Nsp zero.
+ * Rows NE..NEp-1 are not written (zero them once).  Nch <= 2048.  All
+ * buffers 16-byte aligned. */
+MDT_API mdt_status mdt_fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                   const float *window, void *X16, int ab_fmt, float scale,
+                                   cudaStream_t stream);
+
+/* Tensor-core Hermitian X-engine (tcgen05.mma kind::f16, FP32 accumulate)
+ * on the X16 layout above: V_c = X_c X_c^H / (Nsp * scale^2), lower-triangle
+ * tiles only, written full square column-major to `vis` (complex64
+ * [Nch][NE*NE], may be NULL) and/or added to `vis_acc` (complex128, may be
+ * NULL).  `err` (device int) is set to 1 if a bounded device-side wait gave
+ * up.  Replaces cublasCgemmBatched (reference MDT_OneStation_client.cu:1128)
+ * for the reduced-precision path. */
+MDT_API mdt_status mdt_xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt,
+                                  float scale, void *vis, void *vis_acc, int *err,
+                                  cudaStream_t stream);
+
 /* Deterministic synthetic int8 I/Q stream (integer-only arithmetic; same
  * samples as the CPU generator used by the tests): spectra s0 .. s0+nsp-1,
  * element noise sigma_q8[e]/256 LSB, optional tone table tone_q16[e][c][2]
@@ -160,7 +191,7 @@ MDT_API mdt_status mdt_synth_iq(uint64_t seed, int ne, int nch, long s0, long ns
 typedef enum {
     MDT_PREC_FP32 = 0, /* complex64 F-output, FP32 SIMT X-engine (<=1e-5 vs FP64) */
     MDT_PREC_FP16 = 1, /* f16 F-output (power-of-two scaled), tcgen05 X-engine, FP32
-                          accumulate (<=1e-3 vs FP64); Nch <= 4096 */
+                          accumulate (<=1e-3 vs FP64); Nch <= 2048 */
     MDT_PREC_BF16 = 2  /* as FP16 with bf16 operands */
 } mdt_precision;
 

@@ -55,6 +55,9 @@ def _declare(L):
         "mdt_fft_c2c": ([_P, _P, _L, _I, _I, _P], _I),
         "mdt_xengine_f32": ([_I, _I, _I, _P, _L, _L, _F, _P, _P], _I),
         "mdt_fengine_f32": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
+        "mdt_fengine_x16": ([_I, _I, _I, _I, _P, _P, _P, _I, _F, _P], _I),
+        "mdt_fengine_c64b": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
+        "mdt_xengine_tc": ([_I, _I, _I, _P, _I, _F, _P, _P, _P, _P], _I),
         "mdt_synth_iq": ([ctypes.c_uint64, _I, _I, _L, _L, _P, _P, _I, _P, _P, _P, _P], _I),
         "mdt_fx_create": ([_P, ctypes.POINTER(_P)], _I),
         "mdt_fx_destroy": ([_P], _I),
@@ -243,6 +246,27 @@ def xengine_f32(ne, nch, nsp, X, ld, xstride, alpha, V, stream=None):
 def fengine_f32(ne, nch, ntaps, nsp, iq, window, X, stream=None):
     check(lib().mdt_fengine_f32(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X),
                                 stream_handle(stream)), "fengine_f32")
+
+
+def fengine_c64b(ne, nch, ntaps, nsp, iq, window, XB, stream=None):
+    check(lib().mdt_fengine_c64b(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(XB),
+                                 stream_handle(stream)), "fengine_c64b")
+
+
+def fengine_x16(ne, nch, ntaps, nsp, iq, window, X16, ab_fmt=0, scale=1.0, stream=None):
+    check(lib().mdt_fengine_x16(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X16), ab_fmt,
+                                scale, stream_handle(stream)), "fengine_x16")
+
+
+def xengine_tc(ne, nch, nsp, X16, vis, vis_acc=None, err=None, ab_fmt=0, scale=1.0,
+               stream=None):
+    check(lib().mdt_xengine_tc(ne, nch, nsp, ptr(X16), ab_fmt, scale, ptr(vis), ptr(vis_acc),
+                               ptr(err), stream_handle(stream)), "xengine_tc")
+
+
+def x16_bytes(ne, nch, nsp):
+    """Size of the X16 tensor-core operand buffer."""
+    return nch * ((nsp + 31) // 32) * ((ne + 15) // 16 * 16) * 128
 
 
 def synth_iq(seed, ne, nch, s0, nsp, sigma_q8, out, tone_q16=None, src_sigma_q8=None,

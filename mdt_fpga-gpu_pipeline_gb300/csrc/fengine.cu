@@ -23,27 +23,37 @@
 
 namespace mdt {
 
-// Rows (elements) per block of the FP32 F-engine.  Small blocks let several
-// blocks share an SM, so one block's sample loads overlap another's FFT
-// passes and barriers.
+// Rows (elements) per block of the FP32 F-engine and threads per row.
+// Small blocks let several blocks share an SM, so one block's sample loads
+// overlap another's FFT passes and barriers.
 #ifndef MDT_FENG_ROWS
 #define MDT_FENG_ROWS 4
 #endif
+#ifndef MDT_FENG_TPR
+#define MDT_FENG_TPR 256
+#endif
 // Threads per SM the register budget is sized for (64K registers / this).
 #ifndef MDT_FENG_SM_THREADS
-#define MDT_FENG_SM_THREADS 1536
+#define MDT_FENG_SM_THREADS 1024
 #endif
+
+// Threads per row: N/8 (one radix-8 butterfly each) capped at `cap`, but
+// never fewer than N/16 (at most two butterflies per thread and pass).
+constexpr int feng_tpr(int n, int cap)
+{
+    return (n / 8 < 1) ? 1 : (n / 8 <= cap ? n / 8 : (cap >= n / 16 ? cap : n / 16));
+}
 
 template <int N>
 struct FengCfg {
-    static constexpr int TPR = fft::Shape<N>::TPR;
+    static constexpr int TPR = feng_tpr(N, MDT_FENG_TPR);
     static constexpr int RMAX = (1024 / TPR) < 1 ? 1 : 1024 / TPR;
     static constexpr int ROWS = MDT_FENG_ROWS < RMAX ? MDT_FENG_ROWS : RMAX;
     static constexpr int THREADS = ROWS * TPR;
     // resident blocks per SM requested from the register allocator
     static constexpr int MINB = (MDT_FENG_SM_THREADS / THREADS) < 1 ? 1 : (MDT_FENG_SM_THREADS / THREADS);
-    static constexpr int RSTRIDE = 2 * fft::Shape<N>::PADN + 8;  // floats per row (bank skew)
-    static constexpr size_t SMEM = sizeof(float) * (size_t)RSTRIDE * ROWS;
+    static constexpr int RSTRIDE = fft::Shape<N>::PADN + 4;  // float2 per row (bank skew)
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)RSTRIDE * ROWS;
 };
 
 struct FengArgs {
@@ -56,14 +66,14 @@ struct FengArgs {
     float2 *X;
 };
 
-// Polyphase tap sum of the block's ROWS rows into shared memory (natural
-// channel order, padded): each work item is 8 consecutive channels of one
-// row, read as one 16-byte int8 I/Q vector and two float4 window vectors per
-// tap; accumulation is fmaf from zero in increasing tap order.
-// Row r of the block is (spectrum s0, element e0 + r), or with SPECTRA_ROWS
-// (spectrum s0 + r, element e0); rows past NE or Nsp are zero.
+// Polyphase tap sum of the block's rows into shared memory (natural channel
+// order, padded): each work item is 8 consecutive channels of one row, read
+// as one 16-byte int8 I/Q vector and two float4 window vectors per tap;
+// accumulation is fmaf from zero in increasing tap order.  Row r of the block
+// is (spectrum s0, element e0 + r), or with SPECTRA_ROWS (spectrum s0 + r,
+// element e0); rows past NE or Nsp are zero.
 template <int N, int ROWS, int THREADS, bool SPECTRA_ROWS = false>
-__device__ __forceinline__ void pfb_rows_to_smem(const FengArgs &a, int s0, int e0, float *smem,
+__device__ __forceinline__ void pfb_rows_to_smem(const FengArgs &a, int s0, int e0, float2 *smem,
                                                  int rstride)
 {
     constexpr int ITEMS = ROWS * (N / 8);
@@ -98,14 +108,10 @@ __device__ __forceinline__ void pfb_rows_to_smem(const FengArgs &a, int s0, int 
                 }
             }
         }
-        float *sre = smem + (size_t)r * rstride;
-        float *sim = sre + fft::Shape<N>::PADN;
-        const int p0 = fft::pad(c0);  // c0 % 8 == 0: pad(c0 + k) = p0 + k
+        float2 *sx = smem + (size_t)r * rstride;
+        const int p0 = fft::pad(c0);  // c0 % 8 == 0: pad(c0 + k) = p0 + k for k < 8
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            sre[p0 + k] = re[k];
-            sim[p0 + k] = im[k];
-        }
+        for (int k = 0; k < 8; k++) sx[p0 + k] = make_float2(re[k], im[k]);
     }
 }
 
@@ -113,20 +119,19 @@ template <int N>
 __global__ void __launch_bounds__(FengCfg<N>::THREADS, FengCfg<N>::MINB) fengine_f32_kernel(FengArgs a)
 {
     using C = FengCfg<N>;
-    extern __shared__ float smem[];
+    extern __shared__ float2 fsm[];
     const long blk = blockIdx.x;
     const int s = (int)(blk / a.ngroups);
     const int e0 = (int)(blk - (long)s * a.ngroups) * C::ROWS;
     const int lrow = threadIdx.x / C::TPR;
     const int t = threadIdx.x - lrow * C::TPR;
-    float *sre = smem + (size_t)lrow * C::RSTRIDE;
-    float *sim = sre + fft::Shape<N>::PADN;
 
-    pfb_rows_to_smem<N, C::ROWS, C::THREADS>(a, s, e0, smem, C::RSTRIDE);
+    pfb_rows_to_smem<N, C::ROWS, C::THREADS>(a, s, e0, fsm, C::RSTRIDE);
     __syncthreads();
     auto none_load = [](int) { return make_float2(0.f, 0.f); };
     auto none_store = [](int, float2) {};
-    fft::transform_row<N, C::TPR, false, false>(sre, sim, t, a.tw, none_load, none_store);
+    fft::transform_row<N, C::TPR, false, false>(fsm + (size_t)lrow * C::RSTRIDE, t, a.tw,
+                                                none_load, none_store);
 
     // corner turn: ROWS contiguous elements per channel
     const int nrow = min(C::ROWS, a.ne - e0);
@@ -134,145 +139,302 @@ __global__ void __launch_bounds__(FengCfg<N>::THREADS, FengCfg<N>::MINB) fengine
     const long cstride = (long)a.nsp * a.ne;
     for (int k = threadIdx.x; k < N * C::ROWS; k += C::THREADS) {
         const int c = k / C::ROWS, r = k - c * C::ROWS;
-        if (r < nrow) {
-            const float *rr = smem + (size_t)r * C::RSTRIDE;
-            dst[(long)c * cstride + r] =
-                make_float2(rr[fft::pad(c)], rr[fft::Shape<N>::PADN + fft::pad(c)]);
-        }
+        if (r < nrow) dst[(long)c * cstride + r] = fsm[(size_t)r * C::RSTRIDE + fft::pad(c)];
     }
 }
 
 // ------------------------------------------------------------------------
-// F-engine for the tensor-core X-engine: same tap sum and FFT, output scaled
-// by a power of two and rounded to f16 / bf16 in the X16 operand layout of
-// xengine_tc.cu:  X16[c][kc][e][128 B], row = [re(32 spectra) | im(32 spectra)],
-// 16-byte chunk j stored at j ^ (e & 7).  A block owns one element and SB
-// consecutive spectra (SB = 32 when Nch <= 1024), transforms them R rows at a
-// time, stages the rounded values per channel in shared memory and writes
-// whole swizzled chunks.
+// Spectrum-block F-engines (the plan's FP32 path and the tensor-core path).
+// A block owns one element and 8 consecutive spectra s0..s0+7, the rows of
+// its transform.  The tap sum keeps the window of the thread's channels in
+// registers and converts each input spectrum from int8 once: input spectrum
+// s0+j feeds row r at tap j-r, and the unrolled loop over j visits every
+// row's taps in increasing order, so each output is the same fmaf chain as
+// PpS_Batch (bit-identical).  NT is Ntaps as a compile-time constant (4 or
+// 8); other tap counts use the per-row tap sum above.  Consecutive blocks
+// are the four 8-spectrum groups of one (element, 32-spectrum chunk), so
+// their inputs overlap in L2 and their partial output rows meet there.
+
+// Threads per row and register budget of the spectrum-block kernels.
+#ifndef MDT_FENG16_TPR
+#define MDT_FENG16_TPR 64
+#endif
+#ifndef MDT_FENG16_SM_THREADS
+#define MDT_FENG16_SM_THREADS 1024
+#endif
+
+constexpr int SB8 = 8;  // spectra per block
+
 template <int N>
-struct Feng16Cfg {
-    static constexpr int TPR = fft::Shape<N>::TPR;
-    static constexpr int SB = (32 * N * 4 <= 131072) ? 32 : 131072 / (N * 4);
-    static constexpr int RMAX = (1024 / TPR) < 1 ? 1 : 1024 / TPR;
-    static constexpr int R = SB < RMAX ? SB : RMAX;
-    static constexpr int THREADS = R * TPR;
-    static constexpr int RSTRIDE = 2 * fft::Shape<N>::PADN + 8;
-    static constexpr int SROWW = SB + 1;  // staging words per channel row: 2*SB halves + pad
-    static constexpr size_t FFT_SMEM = sizeof(float) * (size_t)RSTRIDE * R;
-    static constexpr size_t SMEM = FFT_SMEM + sizeof(uint32_t) * (size_t)SROWW * N;
+struct FengBCfg {
+    static constexpr int TPR = feng_tpr(N, MDT_FENG16_TPR);
+    static constexpr int THREADS = SB8 * TPR;
+    static constexpr int MINB =
+        (MDT_FENG16_SM_THREADS / THREADS) < 1 ? 1 : (MDT_FENG16_SM_THREADS / THREADS);
+    static constexpr int RSTRIDE = fft::Shape<N>::PADN + 4;
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)RSTRIDE * SB8;
 };
 
-template <typename H>
-__device__ __forceinline__ H to_half(float x);
+template <int CPI>
+struct Samples;
 template <>
-__device__ __forceinline__ __half to_half<__half>(float x)
-{
-    return __float2half_rn(x);
-}
+struct Samples<1> {
+    float re[1], im[1];
+    __device__ __forceinline__ void load(const char2 *p, bool ok)
+    {
+        const char2 v = ok ? __ldg(p) : make_char2(0, 0);
+        re[0] = (float)v.x;
+        im[0] = (float)v.y;
+    }
+};
 template <>
-__device__ __forceinline__ __nv_bfloat16 to_half<__nv_bfloat16>(float x)
+struct Samples<2> {
+    float re[2], im[2];
+    __device__ __forceinline__ void load(const char2 *p, bool ok)
+    {
+        const char4 v = ok ? __ldg(reinterpret_cast<const char4 *>(p)) : make_char4(0, 0, 0, 0);
+        re[0] = (float)v.x;
+        im[0] = (float)v.y;
+        re[1] = (float)v.z;
+        im[1] = (float)v.w;
+    }
+};
+
+template <int N, int NT, int THREADS>
+__device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, int e, float2 *smem,
+                                                   int rstride)
 {
-    return __float2bfloat16_rn(x);
+    constexpr int CPI = (N / THREADS >= 2) ? 2 : 1;  // channels per thread item
+    constexpr int ITEMS = N / CPI;
+    const long rowlen = (long)a.ne * N;
+    const int nin = a.nsp + NT - 1;  // input spectra of this integration
+    for (int it = threadIdx.x; it < ITEMS; it += THREADS) {
+        const int c0 = it * CPI;
+        float w[NT][CPI];
+#pragma unroll
+        for (int i = 0; i < NT; i++)
+#pragma unroll
+            for (int k = 0; k < CPI; k++) w[i][k] = __ldg(a.win + (long)i * N + c0 + k);
+        float ar[SB8][CPI], ai[SB8][CPI];
+#pragma unroll
+        for (int r = 0; r < SB8; r++)
+#pragma unroll
+            for (int k = 0; k < CPI; k++) ar[r][k] = ai[r][k] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < SB8 + NT - 1; j++) {
+            const int sp = s0 + j;
+            const char2 *src = (sp < a.nhist) ? a.hist + (long)sp * rowlen
+                                              : a.iq + (long)(sp - a.nhist) * rowlen;
+            Samples<CPI> x;
+            x.load(src + (long)e * N + c0, sp < nin);
+#pragma unroll
+            for (int r = 0; r < SB8; r++) {
+                const int i = j - r;
+                if (i >= 0 && i < NT) {
+#pragma unroll
+                    for (int k = 0; k < CPI; k++) {
+                        ar[r][k] = __fmaf_rn(w[i][k], x.re[k], ar[r][k]);
+                        ai[r][k] = __fmaf_rn(w[i][k], x.im[k], ai[r][k]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < SB8; r++) {
+            const bool live = s0 + r < a.nsp;
+#pragma unroll
+            for (int k = 0; k < CPI; k++)
+                smem[(size_t)r * rstride + fft::pad(c0 + k)] =
+                    live ? make_float2(ar[r][k], ai[r][k]) : make_float2(0.f, 0.f);
+        }
+    }
 }
 
-template <int N, typename H>
-__global__ void __launch_bounds__(Feng16Cfg<N>::THREADS)
-    fengine_x16_kernel(FengArgs a, uint8_t *__restrict__ X16, int nep, int nkc, float scale)
+// Block decode: blockIdx.x = (kc * NE + e) * 4 + jsub, s0 = 32 kc + 8 jsub.
+struct Block8 {
+    int jsub, e, kc, s0;
+    __device__ __forceinline__ explicit Block8(int ne)
+    {
+        jsub = blockIdx.x & 3;
+        const int rest = blockIdx.x >> 2;
+        e = rest % ne;
+        kc = rest / ne;
+        s0 = kc * 32 + jsub * 8;
+    }
+};
+
+// Tap sum + FFT of the block's 8 rows; the spectra stay in shared memory
+// (row r at fsm + r*RSTRIDE, channel c at pad(c)).
+template <int N, int NT>
+__device__ __forceinline__ void fengine_block8(const FengArgs &a, const Block8 &b, float2 *fsm)
 {
-    using C = Feng16Cfg<N>;
-    extern __shared__ float smem[];
-    uint16_t *stage = reinterpret_cast<uint16_t *>(smem + C::FFT_SMEM / sizeof(float));
-    const int nsblk = nkc * (32 / C::SB);
-    const int e = blockIdx.x % a.ne;
-    const int sblk = blockIdx.x / a.ne;
-    const int s0 = sblk * C::SB;
+    using C = FengBCfg<N>;
+    if constexpr (NT > 0)
+        pfb_block8_to_smem<N, NT, C::THREADS>(a, b.s0, b.e, fsm, C::RSTRIDE);
+    else
+        pfb_rows_to_smem<N, SB8, C::THREADS, true>(a, b.s0, b.e, fsm, C::RSTRIDE);
+    __syncthreads();
     const int lrow = threadIdx.x / C::TPR;
     const int t = threadIdx.x - lrow * C::TPR;
-    float *sre = smem + (size_t)lrow * C::RSTRIDE;
-    float *sim = sre + fft::Shape<N>::PADN;
     auto none_load = [](int) { return make_float2(0.f, 0.f); };
     auto none_store = [](int, float2) {};
-    (void)nsblk;
-
-    for (int round = 0; round < C::SB / C::R; round++) {
-        pfb_rows_to_smem<N, C::R, C::THREADS, true>(a, s0 + round * C::R, e, smem, C::RSTRIDE);
-        __syncthreads();
-        fft::transform_row<N, C::TPR, false, false>(sre, sim, t, a.tw, none_load, none_store);
-        for (int it = threadIdx.x; it < N * C::R; it += C::THREADS) {
-            const int r = it % C::R, c = it / C::R;
-            const float *rr = smem + (size_t)r * C::RSTRIDE;
-            const int sl = round * C::R + r;
-            const H hr = to_half<H>(rr[fft::pad(c)] * scale);
-            const H hi = to_half<H>(rr[fft::Shape<N>::PADN + fft::pad(c)] * scale);
-            stage[(size_t)c * 2 * C::SROWW + sl] = *reinterpret_cast<const uint16_t *>(&hr);
-            stage[(size_t)c * 2 * C::SROWW + C::SB + sl] = *reinterpret_cast<const uint16_t *>(&hi);
-        }
-        __syncthreads();
-    }
-
-    // swizzled 16-byte chunks: local chunk u covers halves 8u..8u+7 of the
-    // staged row (re for u < SB/8, im otherwise)
-    const int kc = s0 / 32, soff = s0 % 32;
-    constexpr int NU = C::SB / 4;
-    const uint32_t *sw = reinterpret_cast<const uint32_t *>(stage);
-    uint8_t *rowbase = X16 + (size_t)kc * nep * 128 + (size_t)e * 128;
-    const size_t cstride = (size_t)nkc * nep * 128;
-    for (int it = threadIdx.x; it < N * NU; it += C::THREADS) {
-        const int u = it % NU, c = it / NU;
-        const int j = (u < C::SB / 8) ? (soff / 8 + u) : (4 + soff / 8 + (u - C::SB / 8));
-        const uint32_t *w = sw + (size_t)c * C::SROWW + 4 * u;
-        uint4 v = make_uint4(w[0], w[1], w[2], w[3]);
-        *reinterpret_cast<uint4 *>(rowbase + (size_t)c * cstride + ((j ^ (e & 7)) << 4)) = v;
-    }
+    fft::transform_row<N, C::TPR, false, false>(fsm + (size_t)lrow * C::RSTRIDE, t, a.tw,
+                                                none_load, none_store);
 }
 
-template <int N, typename H>
-static mdt_status launch_feng16(FengArgs a, uint8_t *X16, int nep, int nkc, float scale,
-                                cudaStream_t stream)
+// FP32 output in the 8-spectrum blocked layout of the plan's FP32 path:
+//   XB[c][sb][e][8] complex64, sb = s/8 (ceil(Nsp/8) blocks, spectra past
+//   Nsp zero): per channel one contiguous 64-byte run per block.
+template <int N, int NT>
+__global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
+    fengine_c64b_kernel(FengArgs a, float2 *__restrict__ XB, int nsb)
 {
-    using C = Feng16Cfg<N>;
-    static_assert(C::SMEM <= 232448, "F-engine X16 shared memory");
-    mdt_status st;
-    a.tw = fft_twiddles(N, &st);
-    if (!a.tw) return st;
-    cudaError_t e = cudaFuncSetAttribute(fengine_x16_kernel<N, H>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
-    if (e != cudaSuccess) return cuda_status(e, "fengine_x16 smem attribute");
-    long blocks = (long)a.ne * nkc * (32 / C::SB);
-    if (blocks > 0x7fffffffL) return invalid("fengine_x16: grid too large");
-    fengine_x16_kernel<N, H><<<(unsigned)blocks, C::THREADS, C::SMEM, stream>>>(a, X16, nep, nkc,
-                                                                              scale);
-    return launch_status("fengine_x16_kernel");
+    using C = FengBCfg<N>;
+    extern __shared__ float2 fsm[];
+    const Block8 b(a.ne);
+    const int sb = b.kc * 4 + b.jsub;
+    if (sb >= nsb) return;  // whole block: the last 32-spectrum chunk may hold fewer groups
+    fengine_block8<N, NT>(a, b, fsm);
+    float2 *base = XB + ((size_t)sb * a.ne + b.e) * SB8;
+    const size_t cstride = (size_t)nsb * a.ne * SB8;
+    for (int it = threadIdx.x; it < N * 4; it += C::THREADS) {
+        const int c = it >> 2, q = it & 3;  // q: pair of spectra
+        const float2 v0 = fsm[(size_t)(2 * q) * C::RSTRIDE + fft::pad(c)];
+        const float2 v1 = fsm[(size_t)(2 * q + 1) * C::RSTRIDE + fft::pad(c)];
+        *reinterpret_cast<float4 *>(base + (size_t)c * cstride + 2 * q) =
+            make_float4(v0.x, v0.y, v1.x, v1.y);
+    }
 }
 
+// f16 / bf16 output (power-of-two scaled) in the tensor-core operand layout
+// of xengine_tc.cu:  X16[c][kc][e][128 B], row = [re(32 spectra) | im(32
+// spectra)], 16-byte chunk j stored at j ^ (e & 7).  The block's 8 spectra
+// are one 16-byte chunk of re and one of im per channel, written straight
+// from the transform's shared memory.
 template <typename H>
-static mdt_status fengine_x16_dispatch(int nch, FengArgs a, uint8_t *X16, int nep, int nkc,
-                                       float scale, cudaStream_t stream)
+__device__ __forceinline__ uint32_t pack2(float lo, float hi);
+template <>
+__device__ __forceinline__ uint32_t pack2<__half>(float lo, float hi)
 {
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+template <>
+__device__ __forceinline__ uint32_t pack2<__nv_bfloat16>(float lo, float hi)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+template <int N, int NT, typename H>
+__global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
+    fengine_x16_kernel(FengArgs a, uint8_t *__restrict__ X16, int nep, int nkc, float scale)
+{
+    using C = FengBCfg<N>;
+    extern __shared__ float2 fsm[];
+    const Block8 b(a.ne);
+    fengine_block8<N, NT>(a, b, fsm);
+
+    uint8_t *rowbase = X16 + ((size_t)b.kc * nep + b.e) * 128;
+    const size_t cstride = (size_t)nkc * nep * 128;
+    const int pre = (b.jsub ^ (b.e & 7)) << 4, pim = ((4 + b.jsub) ^ (b.e & 7)) << 4;
+    for (int c = threadIdx.x; c < N; c += C::THREADS) {
+        float2 v[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) v[r] = fsm[(size_t)r * C::RSTRIDE + fft::pad(c)];
+        uint4 ure, uim;
+        ure.x = pack2<H>(v[0].x * scale, v[1].x * scale);
+        ure.y = pack2<H>(v[2].x * scale, v[3].x * scale);
+        ure.z = pack2<H>(v[4].x * scale, v[5].x * scale);
+        ure.w = pack2<H>(v[6].x * scale, v[7].x * scale);
+        uim.x = pack2<H>(v[0].y * scale, v[1].y * scale);
+        uim.y = pack2<H>(v[2].y * scale, v[3].y * scale);
+        uim.z = pack2<H>(v[4].y * scale, v[5].y * scale);
+        uim.w = pack2<H>(v[6].y * scale, v[7].y * scale);
+        uint8_t *row = rowbase + (size_t)c * cstride;
+        *reinterpret_cast<uint4 *>(row + pre) = ure;
+        *reinterpret_cast<uint4 *>(row + pim) = uim;
+    }
+}
+
+// Calls f.run<N, NT>() for the runtime (nch, ntaps).
+template <class F>
+static mdt_status dispatch_block8(int nch, int ntaps, F f)
+{
+#define MDT_NT_CASES(NV)                                                       \
+    case NV:                                                                   \
+        return ntaps == 4 ? f.template run<NV, 4>()                            \
+                          : (ntaps == 8 ? f.template run<NV, 8>() : f.template run<NV, 0>());
     switch (nch) {
-        case 32: return launch_feng16<32, H>(a, X16, nep, nkc, scale, stream);
-        case 64: return launch_feng16<64, H>(a, X16, nep, nkc, scale, stream);
-        case 128: return launch_feng16<128, H>(a, X16, nep, nkc, scale, stream);
-        case 256: return launch_feng16<256, H>(a, X16, nep, nkc, scale, stream);
-        case 512: return launch_feng16<512, H>(a, X16, nep, nkc, scale, stream);
-        case 1024: return launch_feng16<1024, H>(a, X16, nep, nkc, scale, stream);
-        case 2048: return launch_feng16<2048, H>(a, X16, nep, nkc, scale, stream);
-        case 4096: return launch_feng16<4096, H>(a, X16, nep, nkc, scale, stream);
+        MDT_NT_CASES(32)
+        MDT_NT_CASES(64)
+        MDT_NT_CASES(128)
+        MDT_NT_CASES(256)
+        MDT_NT_CASES(512)
+        MDT_NT_CASES(1024)
+        MDT_NT_CASES(2048)
         default: break;
     }
-    set_error("fengine_x16: Nch must be a power of two in [32, 4096]");
+#undef MDT_NT_CASES
+    set_error("F-engine: Nch must be a power of two in [32, 2048] for this path");
     return MDT_ERR_NOT_SUPPORTED;
 }
 
-// ab_fmt 0 = f16, 1 = bf16; X16 sized nch * nkc * nep * 128 bytes, rows
-// >= NE must already be zero (they are never written).
-mdt_status fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
-                       const int8_t *iq, const float *win, void *X16, int nep, int nkc,
-                       int ab_fmt, float scale, cudaStream_t stream)
+template <typename H>
+struct Feng16Run {
+    FengArgs a;
+    uint8_t *X16;
+    int nep, nkc;
+    float scale;
+    cudaStream_t stream;
+    template <int N, int NT>
+    mdt_status run()
+    {
+        using C = FengBCfg<N>;
+        static_assert(C::SMEM <= 232448, "F-engine shared memory");
+        mdt_status st;
+        a.tw = fft_twiddles(N, &st);
+        if (!a.tw) return st;
+        cudaError_t e = cudaFuncSetAttribute(fengine_x16_kernel<N, NT, H>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)C::SMEM);
+        if (e != cudaSuccess) return cuda_status(e, "fengine_x16 smem attribute");
+        long blocks = (long)a.ne * nkc * 4;
+        if (blocks > 0x7fffffffL) return invalid("fengine_x16: grid too large");
+        fengine_x16_kernel<N, NT, H><<<(unsigned)blocks, C::THREADS, C::SMEM, stream>>>(
+            a, X16, nep, nkc, scale);
+        return launch_status("fengine_x16_kernel");
+    }
+};
+
+struct FengBRun {
+    FengArgs a;
+    float2 *XB;
+    int nsb;
+    cudaStream_t stream;
+    template <int N, int NT>
+    mdt_status run()
+    {
+        using C = FengBCfg<N>;
+        static_assert(C::SMEM <= 232448, "F-engine shared memory");
+        mdt_status st;
+        a.tw = fft_twiddles(N, &st);
+        if (!a.tw) return st;
+        cudaError_t e = cudaFuncSetAttribute(fengine_c64b_kernel<N, NT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)C::SMEM);
+        if (e != cudaSuccess) return cuda_status(e, "fengine_c64b smem attribute");
+        const long nkc = (nsb + 3) / 4;
+        long blocks = (long)a.ne * nkc * 4;
+        if (blocks > 0x7fffffffL) return invalid("fengine_c64b: grid too large");
+        fengine_c64b_kernel<N, NT><<<(unsigned)blocks, C::THREADS, C::SMEM, stream>>>(a, XB, nsb);
+        return launch_status("fengine_c64b_kernel");
+    }
+};
+
+static FengArgs make_args(int ne, int ntaps, int nsp, const int8_t *hist, int nhist,
+                          const int8_t *iq, const float *win)
 {
-    if (((uintptr_t)iq | (uintptr_t)hist | (uintptr_t)win | (uintptr_t)X16) & 15)
-        return invalid("fengine_x16: buffers must be 16-byte aligned");
     FengArgs a;
     a.hist = reinterpret_cast<const char2 *>(hist);
     a.iq = reinterpret_cast<const char2 *>(iq);
@@ -283,11 +445,36 @@ mdt_status fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *hist, 
     a.win = win;
     a.X = nullptr;
     a.ngroups = 0;
-    if (ab_fmt == 1)
-        return fengine_x16_dispatch<__nv_bfloat16>(nch, a, (uint8_t *)X16, nep, nkc, scale, stream);
-    return fengine_x16_dispatch<__half>(nch, a, (uint8_t *)X16, nep, nkc, scale, stream);
+    a.tw = nullptr;
+    return a;
 }
 
+// ab_fmt 0 = f16, 1 = bf16; X16 sized nch * nkc * nep * 128 bytes, rows
+// >= NE must already be zero (they are never written).
+mdt_status fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
+                       const int8_t *iq, const float *win, void *X16, int nep, int nkc,
+                       int ab_fmt, float scale, cudaStream_t stream)
+{
+    if (((uintptr_t)iq | (uintptr_t)hist | (uintptr_t)win | (uintptr_t)X16) & 15)
+        return invalid("fengine_x16: buffers must be 16-byte aligned");
+    FengArgs a = make_args(ne, ntaps, nsp, hist, nhist, iq, win);
+    if (ab_fmt == 1)
+        return dispatch_block8(nch, ntaps,
+                               Feng16Run<__nv_bfloat16>{a, (uint8_t *)X16, nep, nkc, scale, stream});
+    return dispatch_block8(nch, ntaps, Feng16Run<__half>{a, (uint8_t *)X16, nep, nkc, scale, stream});
+}
+
+// FP32 F-engine into the 8-spectrum blocked layout XB (fengine_c64b_kernel).
+mdt_status fengine_c64b(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
+                        const int8_t *iq, const float *win, float2 *XB, cudaStream_t stream)
+{
+    if (((uintptr_t)iq | (uintptr_t)hist | (uintptr_t)win | (uintptr_t)XB) & 15)
+        return invalid("fengine_c64b: buffers must be 16-byte aligned");
+    FengArgs a = make_args(ne, ntaps, nsp, hist, nhist, iq, win);
+    return dispatch_block8(nch, ntaps, FengBRun{a, XB, (nsp + 7) / 8, stream});
+}
+
+// ------------------------------------------------------------------------
 template <int N>
 static mdt_status launch_feng(FengArgs a, cudaStream_t stream)
 {
@@ -353,6 +540,29 @@ mdt_status check_dims(int ne, int nch, int ntaps, int nsp)
 }
 
 }  // namespace mdt
+
+extern "C" MDT_API mdt_status mdt_fengine_x16(int ne, int nch, int ntaps, int nsp,
+                                              const int8_t *iq, const float *window, void *X16,
+                                              int ab_fmt, float scale, cudaStream_t stream)
+{
+    mdt_status st = mdt::check_dims(ne, nch, ntaps, nsp);
+    if (st != MDT_SUCCESS) return st;
+    if (!iq || !window || !X16 || (ab_fmt != 0 && ab_fmt != 1) || !(scale > 0.0f))
+        return mdt::invalid("fengine_x16: bad arguments");
+    const int nep = (ne + 15) / 16 * 16, nkc = (nsp + 31) / 32;
+    return mdt::fengine_x16(ne, nch, ntaps, nsp, nullptr, 0, iq, window, X16, nep, nkc, ab_fmt,
+                            scale, stream);
+}
+
+extern "C" MDT_API mdt_status mdt_fengine_c64b(int ne, int nch, int ntaps, int nsp,
+                                               const int8_t *iq, const float *window, void *XB,
+                                               cudaStream_t stream)
+{
+    mdt_status st = mdt::check_dims(ne, nch, ntaps, nsp);
+    if (st != MDT_SUCCESS) return st;
+    if (!iq || !window || !XB) return mdt::invalid("fengine_c64b: null pointer");
+    return mdt::fengine_c64b(ne, nch, ntaps, nsp, nullptr, 0, iq, window, (float2 *)XB, stream);
+}
 
 extern "C" MDT_API mdt_status mdt_fengine_f32(int ne, int nch, int ntaps, int nsp,
                                               const int8_t *iq, const float *window, void *X,

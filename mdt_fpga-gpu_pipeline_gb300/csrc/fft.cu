@@ -55,7 +55,7 @@ struct RowsCfg {
     static constexpr int TPR = fft::Shape<N>::TPR;
     static constexpr int ROWS = (256 / TPR) < 1 ? 1 : 256 / TPR;
     static constexpr int THREADS = ROWS * TPR;
-    static constexpr size_t SMEM = sizeof(float) * 2 * fft::Shape<N>::PADN * ROWS;
+    static constexpr size_t SMEM = sizeof(float2) * fft::Shape<N>::PADN * ROWS;
 };
 
 template <int N>
@@ -64,13 +64,12 @@ __global__ void __launch_bounds__(RowsCfg<N>::THREADS)
                     int inverse)
 {
     using C = RowsCfg<N>;
-    extern __shared__ float smem[];
+    extern __shared__ float2 smem2[];
     const int lrow = threadIdx.x / C::TPR;
     const int t = threadIdx.x - lrow * C::TPR;
     const long row = (long)blockIdx.x * C::ROWS + lrow;
     const bool valid = row < rows;
-    float *sre = smem + (size_t)lrow * 2 * fft::Shape<N>::PADN;
-    float *sim = sre + fft::Shape<N>::PADN;
+    float2 *sx = smem2 + (size_t)lrow * fft::Shape<N>::PADN;
     const float2 *src = in + (valid ? row : 0) * (long)N;
     float2 *dst = out + (valid ? row : 0) * (long)N;
     auto load = [&](int i) -> float2 {
@@ -80,7 +79,7 @@ __global__ void __launch_bounds__(RowsCfg<N>::THREADS)
     auto store = [&](int i, float2 v) {
         if (valid) dst[i] = inverse ? cconj(v) : v;
     };
-    fft::transform_row<N, C::TPR, true, true>(sre, sim, t, tw, load, store);
+    fft::transform_row<N, C::TPR, true, true>(sx, t, tw, load, store);
 }
 
 template <int N>

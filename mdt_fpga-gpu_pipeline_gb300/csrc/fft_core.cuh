@@ -13,8 +13,10 @@
 // row in natural order and the last pass writes it in natural order, so the
 // first pass can take its inputs from any producer (global memory, the PFB
 // tap sum) and the last pass can hand its outputs to any consumer.
-// Intermediate passes exchange through shared memory, real and imaginary
-// parts in separate padded arrays (index i + i/8) to spread banks.
+// Intermediate passes exchange through shared memory as interleaved float2
+// (one 8-byte access per complex value) at padded index i + i/16, which
+// keeps every pass's warp accesses at the minimum two wavefronts for the
+// strides the passes use.
 // All arithmetic uses explicitly rounded intrinsics so every instantiation
 // of the core produces bit-identical results.
 #pragma once
@@ -32,7 +34,7 @@ namespace fft {
 constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
 constexpr int ipow8(int p) { return p == 0 ? 1 : 8 * ipow8(p - 1); }
 
-__host__ __device__ constexpr int pad(int i) { return i + (i >> 3); }
+__host__ __device__ constexpr int pad(int i) { return i + (i >> 4); }
 
 template <int N>
 struct Shape {
@@ -41,7 +43,7 @@ struct Shape {
     static constexpr int REM = L % 3;    // final radix-2^REM pass if REM > 0
     static constexpr int NPASS = P8 + (REM ? 1 : 0);
     static constexpr int TPR = (N / 8 < 1) ? 1 : ((N / 8 > 1024) ? 1024 : N / 8);  // threads per row
-    static constexpr int PADN = pad(N);  // floats per padded real or imag array
+    static constexpr int PADN = pad(N);  // float2 slots of one padded row
 };
 
 constexpr float kRsqrt2 = 0.70710678118654752440f;
@@ -107,9 +109,9 @@ __device__ __forceinline__ void dft<8>(float2 *v)
 //   so no barrier is needed before the pass writes shared memory.
 // STOREFN (last pass only): outputs go to store(i, v) instead of shared memory.
 // Padded indices are formed from the pass's compile-time strides where the
-// strides are multiples of 8 (pad(x + 8k) = pad(x) + 9k).
+// strides are multiples of 16 (pad(x + 16k) = pad(x) + 17k).
 template <int N, int TPR, int P, bool LOADFN, bool STOREFN, class Load, class Store>
-__device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
+__device__ __forceinline__ void stockham_pass(float2 *sx, int t,
                                               const float2 *__restrict__ tw, Load &load,
                                               Store &store)
 {
@@ -128,8 +130,8 @@ __device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
                 if constexpr (LOADFN) {
                     v[k][m] = load(idx);
                 } else {
-                    const int pi = (NB % 8 == 0) ? pad(b) + m * pad(NB) : pad(idx);
-                    v[k][m] = make_float2(sre[pi], sim[pi]);
+                    const int pi = (NB % 16 == 0) ? pad(b) + m * pad(NB) : pad(idx);
+                    v[k][m] = sx[pi];
                 }
             }
             if constexpr (NS > 1) {
@@ -171,9 +173,8 @@ __device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
                 if constexpr (STOREFN) {
                     store(o, v[k][m]);
                 } else {
-                    const int po = (NS % 8 == 0) ? pad(base) + m * pad(NS) : pad(o);
-                    sre[po] = v[k][m].x;
-                    sim[po] = v[k][m].y;
+                    const int po = (NS % 16 == 0) ? pad(base) + m * pad(NS) : pad(o);
+                    sx[po] = v[k][m];
                 }
             }
         }
@@ -182,28 +183,25 @@ __device__ __forceinline__ void stockham_pass(float *sre, float *sim, int t,
 }
 
 template <int N, int TPR, int P, bool LOADFN, bool STOREFN, class Load, class Store>
-__device__ __forceinline__ void run_passes(float *sre, float *sim, int t,
-                                           const float2 *__restrict__ tw, Load &load,
-                                           Store &store)
+__device__ __forceinline__ void run_passes(float2 *sx, int t, const float2 *__restrict__ tw,
+                                           Load &load, Store &store)
 {
     constexpr int NP = Shape<N>::NPASS;
-    stockham_pass<N, TPR, P, LOADFN && P == 0, STOREFN && P == NP - 1>(sre, sim, t, tw, load,
-                                                                       store);
-    if constexpr (P + 1 < NP)
-        run_passes<N, TPR, P + 1, LOADFN, STOREFN>(sre, sim, t, tw, load, store);
+    stockham_pass<N, TPR, P, LOADFN && P == 0, STOREFN && P == NP - 1>(sx, t, tw, load, store);
+    if constexpr (P + 1 < NP) run_passes<N, TPR, P + 1, LOADFN, STOREFN>(sx, t, tw, load, store);
 }
 
 // Transforms one row: first-pass inputs from load(i) (LOADFN) or from the
-// row's shared arrays in natural order (then the caller must have written
+// row's shared slots in natural order (then the caller must have written
 // them and synchronised), natural-order outputs to store(i, v) (STOREFN) or
-// left in the shared arrays.  sre/sim: the row's arrays of Shape<N>::PADN
-// floats, element i at pad(i).
+// left in shared memory.  sx: the row's Shape<N>::PADN float2 slots,
+// element i at pad(i).  TPR threads per row; when TPR < N/8 each thread
+// handles several butterflies per pass.
 template <int N, int TPR, bool LOADFN, bool STOREFN, class Load, class Store>
-__device__ __forceinline__ void transform_row(float *sre, float *sim, int t,
-                                              const float2 *__restrict__ tw, Load &load,
-                                              Store &store)
+__device__ __forceinline__ void transform_row(float2 *sx, int t, const float2 *__restrict__ tw,
+                                              Load &load, Store &store)
 {
-    run_passes<N, TPR, 0, LOADFN, STOREFN>(sre, sim, t, tw, load, store);
+    run_passes<N, TPR, 0, LOADFN, STOREFN>(sx, t, tw, load, store);
 }
 
 }  // namespace fft

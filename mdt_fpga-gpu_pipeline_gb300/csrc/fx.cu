@@ -18,7 +18,9 @@ mdt_status fengine_f32(int ne, int nch, int ntaps, int nsp, const int8_t *hist, 
 mdt_status xengine_herm_f32(int ne, long nbatch, int nsp, const float2 *X,
                             const float2 *const *Xptrs, long ld, long xstride, float2 *V,
                             float2 *const *Vptrs, long ldv, long vstride, float2 alpha,
-                            float2 beta, bool beta_zero, cudaStream_t stream);
+                            float2 beta, bool beta_zero, cudaStream_t stream, int blocked);
+mdt_status fengine_c64b(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
+                        const int8_t *iq, const float *win, float2 *XB, cudaStream_t stream);
 const float2 *fft_twiddles(int n, mdt_status *st);
 mdt_status fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
                        const int8_t *iq, const float *win, void *X16, int nep, int nkc,
@@ -119,16 +121,34 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
     }
     mdt_status st;
     if (d.precision == MDT_PREC_FP32) {
-        st = mdt::fengine_f32(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
-                              p->window, p->X, p->stream);
-        if (st != MDT_SUCCESS) return st;
-        if (t1) cudaEventRecord(t1, p->stream);
-        // X[c][s][e]: channel c operand is NE x Nsp column-major, ld = NE
-        st = mdt::xengine_herm_f32(d.nelements, d.nchannels, d.nspectra, p->X, nullptr,
-                                   d.nelements, (long)d.nspectra * d.nelements, (float2 *)vis,
-                                   nullptr, d.nelements, (long)d.nelements * d.nelements,
-                                   make_float2(1.0f / d.nspectra, 0.f), make_float2(0.f, 0.f),
-                                   true, p->stream);
+        // F-output in the 8-spectrum blocked layout XB[c][s/8][e][s%8]
+        const long nsb = (d.nspectra + 7) / 8;
+        if (d.nchannels <= 2048)
+            st = mdt::fengine_c64b(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                                   p->window, p->X, p->stream);
+        else
+            st = MDT_ERR_NOT_SUPPORTED;
+        if (st == MDT_ERR_NOT_SUPPORTED) {
+            // Nch > 2048: the element-row F-engine in the ReorderFOutput layout
+            st = mdt::fengine_f32(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist,
+                                  iq, p->window, p->X, p->stream);
+            if (st != MDT_SUCCESS) return st;
+            if (t1) cudaEventRecord(t1, p->stream);
+            st = mdt::xengine_herm_f32(d.nelements, d.nchannels, d.nspectra, p->X, nullptr,
+                                       d.nelements, (long)d.nspectra * d.nelements,
+                                       (float2 *)vis, nullptr, d.nelements,
+                                       (long)d.nelements * d.nelements,
+                                       make_float2(1.0f / d.nspectra, 0.f), make_float2(0.f, 0.f),
+                                       true, p->stream, 0);
+        } else {
+            if (st != MDT_SUCCESS) return st;
+            if (t1) cudaEventRecord(t1, p->stream);
+            st = mdt::xengine_herm_f32(d.nelements, d.nchannels, d.nspectra, p->X, nullptr, 0,
+                                       nsb * 8 * d.nelements, (float2 *)vis, nullptr,
+                                       d.nelements, (long)d.nelements * d.nelements,
+                                       make_float2(1.0f / d.nspectra, 0.f), make_float2(0.f, 0.f),
+                                       true, p->stream, 1);
+        }
         if (st == MDT_SUCCESS && p->acc) {
             long n = (long)d.nchannels * d.nelements * d.nelements;
             mdt::accumulate_f64_kernel<<<(unsigned)std::min<long>(mdt::cdiv(n, 256),
@@ -165,8 +185,8 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
         mdt::set_error("fx_create: precision not supported by this build");
         return MDT_ERR_NOT_SUPPORTED;
     }
-    if (desc->precision != MDT_PREC_FP32 && desc->nchannels > 4096) {
-        mdt::set_error("fx_create: the f16/bf16 path supports Nch <= 4096");
+    if (desc->precision != MDT_PREC_FP32 && desc->nchannels > 2048) {
+        mdt::set_error("fx_create: the f16/bf16 path supports Nch <= 2048");
         return MDT_ERR_NOT_SUPPORTED;
     }
     mdt_fx_plan p = new (std::nothrow) mdt_fx_plan_s;
@@ -178,7 +198,8 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
     size_t hbytes = spectrum_bytes(d) * (size_t)(d.ntaps - 1);
     cudaError_t e = cudaMalloc(&p->window, wbytes);
     if (d.precision == MDT_PREC_FP32) {
-        xbytes = sizeof(float2) * (size_t)d.nspectra * d.nelements * d.nchannels;
+        // room for either layout: blocked pads Nsp up to a multiple of 8
+        xbytes = sizeof(float2) * (size_t)((d.nspectra + 7) / 8 * 8) * d.nelements * d.nchannels;
         if (e == cudaSuccess) e = cudaMalloc(&p->X, xbytes);
     } else {
         p->nep = mdt::x16_padded_rows(d.nelements);

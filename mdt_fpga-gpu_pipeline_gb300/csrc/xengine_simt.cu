@@ -11,7 +11,9 @@
 // channel; each thread accumulates a 4x4 complex micro-tile.  Only micro-tiles
 // on or below the diagonal are computed in diagonal pairs.  When a pair has
 // fewer than 256 micro-tiles the spare threads split the K (time) loop and
-// the partial sums are added in a fixed order.
+// the partial sums are added in a fixed order.  Operand chunks of 32 time
+// samples are staged with cp.async into a double buffer (one barrier pair
+// per chunk, no staging registers).
 #include <cublas_v2.h>
 #include "mdt_cufft_cublas_shim.h"  // checks the exported signatures
 
@@ -26,6 +28,7 @@ constexpr int XS_ST = 64;       // super-tile width
 constexpr int XS_MT = 4;        // micro-tile width
 constexpr int XS_KC = 32;       // time samples staged per chunk
 constexpr int XS_THREADS = 256;
+constexpr int XS_RS = XS_ST + 2;  // staged row stride (float2): 16-byte aligned rows, bank skew
 
 struct XengArgs {
     int ne, nsp, nsuper, npairs;
@@ -37,6 +40,7 @@ struct XengArgs {
     long ldv, vstride;
     float2 alpha, beta;
     int beta_zero;
+    int blocked;  // operand layout: 0 = X[k*ld + e]; 1 = XB[k/8][e][k%8] (NE rows per block)
 };
 
 __device__ __forceinline__ void pair_index(int p, int &I, int &J)
@@ -49,12 +53,27 @@ __device__ __forceinline__ void pair_index(int p, int &I, int &J)
     J = p - i * (i + 1) / 2;
 }
 
-__global__ void __launch_bounds__(XS_THREADS) xengine_herm_f32_kernel(XengArgs a)
+// 8-byte asynchronous global->shared copy; src_bytes 0 fills zeros.
+__device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_bytes)
 {
-    // one array so that the K-slice reduction can reuse both operand tiles
-    __shared__ __align__(16) float2 sbuf[2][XS_KC][XS_ST];
-    float2(*sA)[XS_ST] = sbuf[0];
-    float2(*sB)[XS_ST] = sbuf[1];
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+constexpr size_t XS_SMEM = sizeof(float2) * 2 /*stages*/ * 2 /*A,B*/ * XS_KC * XS_RS;
+
+__global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArgs a)
+{
+    // [stage][operand][k][element]; the K-slice reduction reuses the space
+    extern __shared__ float4 xs_smem4[];
+    float2 *sbuf = reinterpret_cast<float2 *>(xs_smem4);
+    auto tileA = [&](int st) { return sbuf + (size_t)(st * 2 + 0) * XS_KC * XS_RS; };
+    auto tileB = [&](int st) { return sbuf + (size_t)(st * 2 + 1) * XS_KC * XS_RS; };
 
     const int ch = blockIdx.x / a.npairs;
     const int pr = blockIdx.x - ch * a.npairs;
@@ -79,52 +98,64 @@ __global__ void __launch_bounds__(XS_THREADS) xengine_herm_f32_kernel(XengArgs a
 
     const float2 *Xc = a.Xptrs ? a.Xptrs[ch] : a.X + (long)ch * a.xstride;
 
+    // stage chunk k0 into buffer st: XS_KC x 64 complex per operand, [kk][e]
+    auto stage = [&](int k0, int st) {
+        float2 *A = tileA(st), *B = tileB(st);
+        for (int idx = tid; idx < XS_KC * XS_ST; idx += XS_THREADS) {
+            int kk, e;
+            long off;  // element offset of (k0 + kk, e = 0) in the channel's operand
+            if (a.blocked) {  // consecutive threads: 8 spectra of one element, then the next
+                const int k8 = idx & 7;
+                e = (idx >> 3) & (XS_ST - 1);
+                kk = ((idx >> 9) << 3) + k8;
+                off = ((long)((k0 >> 3) + (idx >> 9)) * a.ne) * 8 + k8;
+            } else {  // consecutive threads: consecutive elements of one time sample
+                kk = idx / XS_ST;
+                e = idx - kk * XS_ST;
+                off = (long)(k0 + kk) * a.ld;
+            }
+            const int es = a.blocked ? 8 : 1;  // element stride
+            const bool kin = k0 + kk < a.nsp;
+            const bool ina = kin && e < nr;
+            float2 *da = A + kk * XS_RS + e;
+            cp_async8(da, ina ? Xc + off + (long)(r0 + e) * es : Xc, ina ? 8 : 0);
+            if (!diag) {
+                const bool inb = kin && e < nq;
+                cp_async8(B + kk * XS_RS + e, inb ? Xc + off + (long)(q0 + e) * es : Xc,
+                          inb ? 8 : 0);
+            }
+        }
+        cp_async_commit();
+    };
+
     float2 acc[XS_MT][XS_MT];
 #pragma unroll
     for (int i = 0; i < XS_MT; i++)
 #pragma unroll
         for (int j = 0; j < XS_MT; j++) acc[i][j] = make_float2(0.f, 0.f);
 
-    // staging: XS_KC x 64 complex per operand, 8 per thread
-    constexpr int PER = XS_KC * XS_ST / XS_THREADS;
-    float2 ra[PER], rb[PER];
-    auto fetch = [&](int k0) {
-#pragma unroll
-        for (int u = 0; u < PER; u++) {
-            int idx = tid + u * XS_THREADS;
-            int kk = idx / XS_ST, e = idx - kk * XS_ST;
-            int k = k0 + kk;
-            bool kin = k < a.nsp;
-            ra[u] = (kin && e < nr) ? Xc[(long)k * a.ld + r0 + e] : make_float2(0.f, 0.f);
-            if (!diag) rb[u] = (kin && e < nq) ? Xc[(long)k * a.ld + q0 + e] : make_float2(0.f, 0.f);
+    const int nchunk = (a.nsp + XS_KC - 1) / XS_KC;
+    stage(0, 0);
+    for (int c = 0; c < nchunk; c++) {
+        const int st = c & 1;
+        if (c + 1 < nchunk) {
+            stage((c + 1) * XS_KC, st ^ 1);
+            cp_async_wait1();
+        } else {
+            cp_async_wait0();
         }
-    };
-    auto stash = [&]() {
-#pragma unroll
-        for (int u = 0; u < PER; u++) {
-            int idx = tid + u * XS_THREADS;
-            int kk = idx / XS_ST, e = idx - kk * XS_ST;
-            sA[kk][e] = ra[u];
-            if (!diag) sB[kk][e] = rb[u];
-        }
-    };
-
-    const float2(*B)[XS_ST] = diag ? sA : sB;
-    fetch(0);
-    for (int k0 = 0; k0 < a.nsp; k0 += XS_KC) {
         __syncthreads();
-        stash();
-        __syncthreads();
-        if (k0 + XS_KC < a.nsp) fetch(k0 + XS_KC);
         if (active) {
+            const float2 *A = tileA(st);
+            const float2 *B = diag ? A : tileB(st);
             for (int kk = ks; kk < XS_KC; kk += ksl) {
-                const float4 *pa = reinterpret_cast<const float4 *>(&sA[kk][mi * XS_MT]);
-                const float4 *pb = reinterpret_cast<const float4 *>(&B[kk][mj * XS_MT]);
-                float4 a01 = pa[0], a23 = pa[1], b01 = pb[0], b23 = pb[1];
-                float2 av[4] = {make_float2(a01.x, a01.y), make_float2(a01.z, a01.w),
-                                make_float2(a23.x, a23.y), make_float2(a23.z, a23.w)};
-                float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w),
-                                make_float2(b23.x, b23.y), make_float2(b23.z, b23.w)};
+                const float4 *pa = reinterpret_cast<const float4 *>(A + kk * XS_RS + mi * XS_MT);
+                const float4 *pb = reinterpret_cast<const float4 *>(B + kk * XS_RS + mj * XS_MT);
+                const float4 a01 = pa[0], a23 = pa[1], b01 = pb[0], b23 = pb[1];
+                const float2 av[4] = {make_float2(a01.x, a01.y), make_float2(a01.z, a01.w),
+                                      make_float2(a23.x, a23.y), make_float2(a23.z, a23.w)};
+                const float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w),
+                                      make_float2(b23.x, b23.y), make_float2(b23.z, b23.w)};
 #pragma unroll
                 for (int i = 0; i < XS_MT; i++)
 #pragma unroll
@@ -137,12 +168,12 @@ __global__ void __launch_bounds__(XS_THREADS) xengine_herm_f32_kernel(XengArgs a
                     }
             }
         }
+        __syncthreads();  // buffer st is overwritten by the next stage() call
     }
 
     // reduce the K slices in a fixed order (slice 0 + 1 + 2 ...)
     if (ksl > 1) {
-        __syncthreads();
-        float2 *red = &sbuf[0][0][0];  // (ksl-1)*nmt*16 < 256*16 complex = both tiles
+        float2 *red = sbuf;  // (ksl-1)*nmt*16 < 256*16 complex
         if (active && ks > 0) {
 #pragma unroll
             for (int i = 0; i < XS_MT; i++)
@@ -203,7 +234,7 @@ __global__ void __launch_bounds__(XS_THREADS) xengine_herm_f32_kernel(XengArgs a
 mdt_status xengine_herm_f32(int ne, long nbatch, int nsp, const float2 *X,
                             const float2 *const *Xptrs, long ld, long xstride, float2 *V,
                             float2 *const *Vptrs, long ldv, long vstride, float2 alpha,
-                            float2 beta, bool beta_zero, cudaStream_t stream)
+                            float2 beta, bool beta_zero, cudaStream_t stream, int blocked)
 {
     if (ne <= 0 || nbatch <= 0) return MDT_SUCCESS;
     XengArgs a;
@@ -222,9 +253,13 @@ mdt_status xengine_herm_f32(int ne, long nbatch, int nsp, const float2 *X,
     a.alpha = alpha;
     a.beta = beta;
     a.beta_zero = beta_zero ? 1 : 0;
+    a.blocked = blocked;
     long blocks = nbatch * a.npairs;
     if (blocks > 0x7fffffffL) return invalid("xengine: grid too large");
-    xengine_herm_f32_kernel<<<(unsigned)blocks, XS_THREADS, 0, stream>>>(a);
+    cudaError_t e = cudaFuncSetAttribute(xengine_herm_f32_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)XS_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "xengine smem attribute");
+    xengine_herm_f32_kernel<<<(unsigned)blocks, XS_THREADS, XS_SMEM, stream>>>(a);
     return launch_status("xengine_herm_f32_kernel");
 }
 
@@ -239,6 +274,7 @@ struct GemmArgs {
     int lda, ldb, ldc;
     float2 alpha, beta;
     int beta_zero;
+    int blocked;  // operand layout: 0 = X[k*ld + e]; 1 = XB[k/8][e][k%8] (NE rows per block)
 };
 
 __device__ __forceinline__ float2 opval(const float2 *M, int ld, int t, int row, int col)
@@ -300,7 +336,7 @@ MDT_API mdt_status mdt_xengine_f32(int ne, int nch, int nsp, const void *X, long
         return mdt::invalid("xengine_f32: bad arguments");
     return mdt::xengine_herm_f32(ne, nch, nsp, (const float2 *)X, nullptr, ld, xstride,
                                  (float2 *)V, nullptr, ne, (long)ne * ne,
-                                 make_float2(alpha, 0.f), make_float2(0.f, 0.f), true, stream);
+                                 make_float2(alpha, 0.f), make_float2(0.f, 0.f), true, stream, 0);
 }
 
 }  // extern "C"
@@ -384,7 +420,7 @@ cublasStatus_t CUBLASWINAPI cublasCgemmBatched(cublasHandle_t handle, cublasOper
         st = mdt::xengine_herm_f32(m, batchCount, k, nullptr,
                                    reinterpret_cast<const float2 *const *>(Aarray), lda, 0,
                                    nullptr, reinterpret_cast<float2 *const *>(Carray), ldc, 0,
-                                   al, be, beta_zero, handle->stream);
+                                   al, be, beta_zero, handle->stream, 0);
     } else {
         if (batchCount > 65535) return CUBLAS_STATUS_NOT_SUPPORTED;
         mdt::GemmArgs g;

@@ -251,3 +251,14 @@ mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, flo
 }
 
 }  // namespace mdt
+
+extern "C" MDT_API mdt_status mdt_xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt,
+                                             float scale, void *vis, void *vis_acc, int *err,
+                                             cudaStream_t stream)
+{
+    if (ne < 1 || ne > MDT_MAX_ELEMENTS || nch < 1 || nsp < 1 || (ab_fmt != 0 && ab_fmt != 1) ||
+        !(scale > 0.0f))
+        return mdt::invalid("xengine_tc: bad arguments");
+    return mdt::xengine_tc(ne, nch, nsp, X16, ab_fmt, scale, (float2 *)vis, (double2 *)vis_acc,
+                           err, stream);
+}

@@ -211,3 +211,25 @@ def test_plan_errors(mdt, cuda):
         plan.execute(iq, 1, vis)  # no window yet
     assert e.value.code == 6
     plan.close()
+
+
+@pytest.mark.parametrize("ne,nch,ntaps,nsp", [(40, 2048, 8, 100), (10, 1024, 4, 64), (5, 256, 6, 9),
+                                              (3, 32, 4, 2)])
+def test_blocked_fengine_matches_reference_layout(mdt, cuda, ne, nch, ntaps, nsp):
+    """The spectrum-block F-engine (8-spectrum blocked layout) gives the same
+    bits as the element-row F-engine (ReorderFOutput layout), for the
+    compile-time tap counts and the runtime-loop fallback (ntaps=6)."""
+    cfg = mdt.configs.small(mdt.configs.C2, nelements=ne, nchannels=nch, ntaps=ntaps,
+                            nspectra=nsp)
+    iq = gen_iq(mdt, cfg, 0, nsp + ntaps - 1)
+    win = window(mdt, nch, ntaps)
+    X = torch.empty(nsp * ne * nch, dtype=torch.complex64, device="cuda")
+    mdt.fengine_f32(ne, nch, ntaps, nsp, iq, win, X)
+    nsb = (nsp + 7) // 8
+    XB = torch.full((nch * nsb * ne * 8,), float("nan"), dtype=torch.complex64, device="cuda")
+    mdt.fengine_c64b(ne, nch, ntaps, nsp, iq, win, XB)
+    torch.cuda.synchronize()
+    xb = XB.view(nch, nsb, ne, 8).permute(0, 1, 3, 2).reshape(nch, nsb * 8, ne)
+    assert torch.all(xb[:, nsp:, :] == 0)
+    ref = X.view(nch, nsp, ne)
+    assert torch.equal(xb[:, :nsp, :].contiguous().view(torch.int64), ref.view(torch.int64))
