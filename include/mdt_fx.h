@@ -260,6 +260,30 @@ MDT_API mdt_status mdt_fx_set_timing(mdt_fx_plan plan, int enable);
 MDT_API mdt_status mdt_fx_get_timing(mdt_fx_plan plan, double *fengine_ms, double *xengine_ms,
                                      int *count);
 
+/* ------------------------------------------------------------------------
+ * One integration without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory
+ * themselves -- a real-time ingest loop in which cudaMalloc's implicit device
+ * synchronisation would stall other streams, a plugin host that fixes the
+ * library's device-memory budget up front, or a foreign-language runtime that
+ * owns every device allocation.
+ *
+ * Runs the plan's FP32 path (int8 I/Q -> spectrum-block F-engine ->
+ * Hermitian X-engine) on `iq` (Nsp + Ntaps - 1 spectra, 16-byte aligned),
+ * `window` (Ntaps*Nch floats, 16-byte aligned) into `vis` (complex64
+ * [Nch][NE*NE], the layout of mdt_fx_execute, which it matches).  The
+ * F-engine output lives in a file-scope device array of 96 MiB
+ * (MDT_STATIC_SCRATCH_BYTES at build time) that every GPU loading the
+ * library holds until exit: requests needing more than that --
+ * Nch * ceil(Nsp/8)*8 * NE * 8 bytes -- or Nch > 2048 return
+ * MDT_ERR_INVALID_VALUE.  The first call on a device (with that device
+ * current) looks up the arrays' device addresses and uploads the FFT
+ * twiddle tables, so make it before any stream capture.  All calls on a
+ * device share the scratch; calls whose GPU work overlaps race on it.
+ * Calls no cudaMalloc/cudaFree. */
+MDT_API mdt_status mdt_fx_integrate_static(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                           const float *window, void *vis, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

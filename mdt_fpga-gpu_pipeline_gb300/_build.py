@@ -19,8 +19,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmdtfx.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Size of the file-scope scratch array of mdt_fx_integrate_static (96 MiB).
+STATIC_SCRATCH_BYTES = 96 << 20
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=default",
-              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills",
+              "-DMDT_STATIC_SCRATCH_BYTES=%d" % STATIC_SCRATCH_BYTES]
 
 
 def nvcc():

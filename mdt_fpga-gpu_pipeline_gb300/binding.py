@@ -69,6 +69,7 @@ def _declare(L):
         "mdt_fx_stream_push": ([_P, _P, _P], _I),
         "mdt_fx_execute_host": ([_P, _P, _I, _P], _I),
         "mdt_fx_set_accumulator": ([_P, _P], _I),
+        "mdt_fx_integrate_static": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
         "mdt_fx_get_scale": ([_P, ctypes.POINTER(ctypes.c_float)], _I),
         "mdt_fx_check": ([_P], _I),
         "mdt_fx_set_timing": ([_P, _I], _I),
@@ -275,6 +276,12 @@ def synth_iq(seed, ne, nch, s0, nsp, sigma_q8, out, tone_q16=None, src_sigma_q8=
     check(lib().mdt_synth_iq(seed, ne, nch, s0, nsp, ptr(sigma_q8), ptr(tone_q16), nsrc,
                              ptr(src_sigma_q8), ptr(src_delay), ptr(out), stream_handle(stream)),
           "synth_iq")
+
+
+def fx_integrate_static(ne, nch, ntaps, nsp, iq, window, vis, stream=None):
+    """One FP32 integration with no device allocation (mdt_fx_integrate_static)."""
+    check(lib().mdt_fx_integrate_static(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(vis),
+                                        stream_handle(stream)), "mdt_fx_integrate_static")
 
 
 # ----------------------------------------------------------- plan API

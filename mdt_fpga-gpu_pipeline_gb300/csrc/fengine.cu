@@ -412,13 +412,17 @@ struct FengBRun {
     float2 *XB;
     int nsb;
     cudaStream_t stream;
+    // optional caller-provided twiddles: the tables for N = 32, 64, ..., 2048
+    // back to back (the table for N starts at entry N - 32); null = the
+    // library's per-device tables
+    const float2 *tw_concat = nullptr;
     template <int N, int NT>
     mdt_status run()
     {
         using C = FengBCfg<N>;
         static_assert(C::SMEM <= 232448, "F-engine shared memory");
-        mdt_status st;
-        a.tw = fft_twiddles(N, &st);
+        mdt_status st = MDT_SUCCESS;
+        a.tw = tw_concat ? tw_concat + (N - 32) : fft_twiddles(N, &st);
         if (!a.tw) return st;
         cudaError_t e = cudaFuncSetAttribute(fengine_c64b_kernel<N, NT>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -472,6 +476,20 @@ mdt_status fengine_c64b(int ne, int nch, int ntaps, int nsp, const int8_t *hist,
         return invalid("fengine_c64b: buffers must be 16-byte aligned");
     FengArgs a = make_args(ne, ntaps, nsp, hist, nhist, iq, win);
     return dispatch_block8(nch, ntaps, FengBRun{a, XB, (nsp + 7) / 8, stream});
+}
+
+// As fengine_c64b, with the twiddle tables supplied by the caller (see
+// FengBRun::tw_concat); allocates nothing.
+mdt_status fengine_c64b_given_twiddles(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                       const float *win, float2 *XB, const float2 *tw_concat,
+                                       cudaStream_t stream)
+{
+    if (((uintptr_t)iq | (uintptr_t)win | (uintptr_t)XB) & 15)
+        return invalid("fengine_c64b: buffers must be 16-byte aligned");
+    FengArgs a = make_args(ne, ntaps, nsp, nullptr, 0, iq, win);
+    FengBRun run{a, XB, (nsp + 7) / 8, stream};
+    run.tw_concat = tw_concat;
+    return dispatch_block8(nch, ntaps, run);
 }
 
 // ------------------------------------------------------------------------
