@@ -163,6 +163,22 @@ MDT_API mdt_status mdt_fengine_x16(int ne, int nch, int ntaps, int nsp, const in
                                    const float *window, void *X16, int ab_fmt, float scale,
                                    cudaStream_t stream);
 
+/* Exact-int8 F-engine: as mdt_fengine_x16 but the values are integers
+ * clamp(rint(x * qscales[c]), -127, 127) (stored as f16, exactly). */
+MDT_API mdt_status mdt_fengine_q8(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                  const float *window, void *X16, const float *qscales,
+                                  cudaStream_t stream);
+
+/* Exact int8 X-engine on tensor cores: X16 holding integers in [-127, 127];
+ * f16 MMAs accumulate 512-spectrum windows in TMEM (exact: every partial sum
+ * is an integer below 2^24) that are folded into int32 running sums.
+ * `vis_i32` (int32 (re, im) [Nch][NE*NE], may be NULL) receives the exact
+ * sums, `vis` (may be NULL) sums / (Nsp * qscales[c]^2), `vis_acc` (may be
+ * NULL) adds them in FP64.  Nsp <= 16384 keeps every sum within int32. */
+MDT_API mdt_status mdt_xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qscales,
+                                  void *vis, void *vis_acc, void *vis_i32, int *err,
+                                  cudaStream_t stream);
+
 /* Tensor-core Hermitian X-engine (tcgen05.mma kind::f16, FP32 accumulate)
  * on the X16 layout above: V_c = X_c X_c^H / (Nsp * scale^2), lower-triangle
  * tiles only, written full square column-major to `vis` (complex64
@@ -192,7 +208,11 @@ typedef enum {
     MDT_PREC_FP32 = 0, /* complex64 F-output, FP32 SIMT X-engine (<=1e-5 vs FP64) */
     MDT_PREC_FP16 = 1, /* f16 F-output (power-of-two scaled), tcgen05 X-engine, FP32
                           accumulate (<=1e-3 vs FP64); Nch <= 2048 */
-    MDT_PREC_BF16 = 2  /* as FP16 with bf16 operands */
+    MDT_PREC_BF16 = 2, /* as FP16 with bf16 operands */
+    MDT_PREC_INT8 = 3  /* F-output requantised per channel to integers in [-127, 127];
+                          exact int32 visibilities on the f16 tensor cores (windowed
+                          FP32-exact accumulation folded into int32), scaled to float;
+                          Nch <= 2048.  (sm_103a has no int8 tensor-core MMA.) */
 } mdt_precision;
 
 typedef struct {
@@ -217,6 +237,13 @@ MDT_API mdt_status mdt_fx_set_window(mdt_fx_plan plan, const float *window);
  * [Nch][NE*NE], 16-byte aligned, zeroed by the caller) is set, every
  * integration's visibilities are also added into it; NULL disables. */
 MDT_API mdt_status mdt_fx_set_accumulator(mdt_fx_plan plan, void *acc);
+/* INT8 plans: per-channel requantisation scales (device, Nch floats).  The
+ * F-output x of channel c becomes clamp(rint(x * scales[c]), -127, 127);
+ * visibilities are the exact integer sums / (Nsp * scales[c]^2).  Without a
+ * call (or after a call with NULL) the plan calibrates them at the next
+ * integration from its first min(Nsp, 64) spectra: scales[c] = 20 / rms_c. */
+MDT_API mdt_status mdt_fx_set_channel_scales(mdt_fx_plan plan, const float *scales);
+MDT_API mdt_status mdt_fx_get_channel_scales(mdt_fx_plan plan, float *scales);
 /* The power-of-two scale applied to the F-engine output before rounding to
  * f16/bf16 (chosen from the window at mdt_fx_set_window; 1 for FP32); the
  * visibilities are divided by scale^2. */

@@ -17,7 +17,7 @@ CUFFT_FORWARD = -1
 CUFFT_INVERSE = 1
 CUFFT_C2C = 0x29
 CUBLAS_OP_N, CUBLAS_OP_T, CUBLAS_OP_C = 0, 1, 2
-MDT_PREC_FP32, MDT_PREC_FP16, MDT_PREC_BF16 = 0, 1, 2
+MDT_PREC_FP32, MDT_PREC_FP16, MDT_PREC_BF16, MDT_PREC_INT8 = 0, 1, 2, 3
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -69,6 +69,10 @@ def _declare(L):
         "mdt_fx_stream_push": ([_P, _P, _P], _I),
         "mdt_fx_execute_host": ([_P, _P, _I, _P], _I),
         "mdt_fx_set_accumulator": ([_P, _P], _I),
+        "mdt_fx_set_channel_scales": ([_P, _P], _I),
+        "mdt_fx_get_channel_scales": ([_P, _P], _I),
+        "mdt_fengine_q8": ([_I, _I, _I, _I, _P, _P, _P, _P, _P], _I),
+        "mdt_xengine_q8": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P], _I),
         "mdt_fx_integrate_static": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
         "mdt_fx_get_scale": ([_P, ctypes.POINTER(ctypes.c_float)], _I),
         "mdt_fx_check": ([_P], _I),
@@ -265,6 +269,17 @@ def xengine_tc(ne, nch, nsp, X16, vis, vis_acc=None, err=None, ab_fmt=0, scale=1
                                ptr(err), stream_handle(stream)), "xengine_tc")
 
 
+def fengine_q8(ne, nch, ntaps, nsp, iq, window, X16, qscales, stream=None):
+    check(lib().mdt_fengine_q8(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X16), ptr(qscales),
+                               stream_handle(stream)), "fengine_q8")
+
+
+def xengine_q8(ne, nch, nsp, X16, qscales, vis=None, vis_acc=None, vis_i32=None, err=None,
+               stream=None):
+    check(lib().mdt_xengine_q8(ne, nch, nsp, ptr(X16), ptr(qscales), ptr(vis), ptr(vis_acc),
+                               ptr(vis_i32), ptr(err), stream_handle(stream)), "xengine_q8")
+
+
 def x16_bytes(ne, nch, nsp):
     """Size of the X16 tensor-core operand buffer."""
     return nch * ((nsp + 31) // 32) * ((ne + 15) // 16 * 16) * 128
@@ -311,6 +326,14 @@ class FxPlan:
     def set_accumulator(self, acc):
         """FP64 cross-integration accumulator (complex128 CUDA tensor) or None."""
         check(lib().mdt_fx_set_accumulator(self._h, ptr(acc)), "mdt_fx_set_accumulator")
+
+    def set_channel_scales(self, scales):
+        """INT8 plans: per-channel requantisation scales (CUDA float tensor) or
+        None to recalibrate at the next integration."""
+        check(lib().mdt_fx_set_channel_scales(self._h, ptr(scales)), "mdt_fx_set_channel_scales")
+
+    def get_channel_scales(self, out):
+        check(lib().mdt_fx_get_channel_scales(self._h, ptr(out)), "mdt_fx_get_channel_scales")
 
     def scale(self):
         v = ctypes.c_float(0)

@@ -326,9 +326,24 @@ __device__ __forceinline__ uint32_t pack2<__nv_bfloat16>(float lo, float hi)
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
-template <int N, int NT, typename H>
+// QUANT: requantise each channel to integers in [-127, 127] with
+// qscales[c] (rint, clamp) before the (exact) conversion to f16 -- the
+// int8 operand of the exact int8 X-engine mode.
+template <bool QUANT>
+__device__ __forceinline__ float prep(float x, float sc)
+{
+    if constexpr (QUANT) {
+        float v = rintf(x * sc);
+        return fminf(fmaxf(v, -127.0f), 127.0f);
+    } else {
+        return x * sc;
+    }
+}
+
+template <int N, int NT, typename H, bool QUANT>
 __global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
-    fengine_x16_kernel(FengArgs a, uint8_t *__restrict__ X16, int nep, int nkc, float scale)
+    fengine_x16_kernel(FengArgs a, uint8_t *__restrict__ X16, int nep, int nkc, float scale,
+                       const float *__restrict__ qscales)
 {
     using C = FengBCfg<N>;
     extern __shared__ float2 fsm[];
@@ -342,19 +357,50 @@ __global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
         float2 v[8];
 #pragma unroll
         for (int r = 0; r < 8; r++) v[r] = fsm[(size_t)r * C::RSTRIDE + fft::pad(c)];
+        const float sc = QUANT ? __ldg(qscales + c) : scale;
         uint4 ure, uim;
-        ure.x = pack2<H>(v[0].x * scale, v[1].x * scale);
-        ure.y = pack2<H>(v[2].x * scale, v[3].x * scale);
-        ure.z = pack2<H>(v[4].x * scale, v[5].x * scale);
-        ure.w = pack2<H>(v[6].x * scale, v[7].x * scale);
-        uim.x = pack2<H>(v[0].y * scale, v[1].y * scale);
-        uim.y = pack2<H>(v[2].y * scale, v[3].y * scale);
-        uim.z = pack2<H>(v[4].y * scale, v[5].y * scale);
-        uim.w = pack2<H>(v[6].y * scale, v[7].y * scale);
+        ure.x = pack2<H>(prep<QUANT>(v[0].x, sc), prep<QUANT>(v[1].x, sc));
+        ure.y = pack2<H>(prep<QUANT>(v[2].x, sc), prep<QUANT>(v[3].x, sc));
+        ure.z = pack2<H>(prep<QUANT>(v[4].x, sc), prep<QUANT>(v[5].x, sc));
+        ure.w = pack2<H>(prep<QUANT>(v[6].x, sc), prep<QUANT>(v[7].x, sc));
+        uim.x = pack2<H>(prep<QUANT>(v[0].y, sc), prep<QUANT>(v[1].y, sc));
+        uim.y = pack2<H>(prep<QUANT>(v[2].y, sc), prep<QUANT>(v[3].y, sc));
+        uim.z = pack2<H>(prep<QUANT>(v[4].y, sc), prep<QUANT>(v[5].y, sc));
+        uim.w = pack2<H>(prep<QUANT>(v[6].y, sc), prep<QUANT>(v[7].y, sc));
         uint8_t *row = rowbase + (size_t)c * cstride;
         *reinterpret_cast<uint4 *>(row + pre) = ure;
         *reinterpret_cast<uint4 *>(row + pim) = uim;
     }
+}
+
+// Per-channel mean power over the elements and spectra of an XB buffer
+// (nsb blocks of 8 spectra, nsp valid): pw[c] = mean |X|^2.
+__global__ void channel_power_kernel(const float2 *__restrict__ XB, int ne, int nsb, int nsp,
+                                     float *__restrict__ pw)
+{
+    const int c = blockIdx.x;
+    const float2 *xc = XB + (size_t)c * nsb * ne * 8;
+    double acc = 0.0;
+    for (long i = threadIdx.x; i < (long)nsb * ne * 8; i += blockDim.x) {
+        const float2 v = xc[i];
+        acc += (double)v.x * v.x + (double)v.y * v.y;
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) pw[c] = (float)(red[0] / ((double)ne * nsp));
+}
+
+// scale[c] = target_rms / sqrt(power[c]) (1 when the channel carries no power).
+__global__ void scales_from_power_kernel(const float *__restrict__ pw, int nch, float target_rms,
+                                         float *__restrict__ scales)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nch) scales[c] = pw[c] > 0.0f ? target_rms / sqrtf(pw[c]) : 1.0f;
 }
 
 // Calls f.run<N, NT>() for the runtime (nch, ntaps).
@@ -387,6 +433,7 @@ struct Feng16Run {
     int nep, nkc;
     float scale;
     cudaStream_t stream;
+    const float *qscales = nullptr;  // non-null: requantise (exact int8 mode)
     template <int N, int NT>
     mdt_status run()
     {
@@ -395,14 +442,13 @@ struct Feng16Run {
         mdt_status st;
         a.tw = fft_twiddles(N, &st);
         if (!a.tw) return st;
-        cudaError_t e = cudaFuncSetAttribute(fengine_x16_kernel<N, NT, H>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)C::SMEM);
-        if (e != cudaSuccess) return cuda_status(e, "fengine_x16 smem attribute");
         long blocks = (long)a.ne * nkc * 4;
         if (blocks > 0x7fffffffL) return invalid("fengine_x16: grid too large");
-        fengine_x16_kernel<N, NT, H><<<(unsigned)blocks, C::THREADS, C::SMEM, stream>>>(
-            a, X16, nep, nkc, scale);
+        auto kern = qscales ? fengine_x16_kernel<N, NT, H, true> : fengine_x16_kernel<N, NT, H, false>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)C::SMEM);
+        if (e != cudaSuccess) return cuda_status(e, "fengine_x16 smem attribute");
+        kern<<<(unsigned)blocks, C::THREADS, C::SMEM, stream>>>(a, X16, nep, nkc, scale, qscales);
         return launch_status("fengine_x16_kernel");
     }
 };
@@ -466,6 +512,34 @@ mdt_status fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *hist, 
         return dispatch_block8(nch, ntaps,
                                Feng16Run<__nv_bfloat16>{a, (uint8_t *)X16, nep, nkc, scale, stream});
     return dispatch_block8(nch, ntaps, Feng16Run<__half>{a, (uint8_t *)X16, nep, nkc, scale, stream});
+}
+
+// Per-channel int8 scales from the power of a blocked FP32 F-output:
+// scale[c] = target_rms / rms_c.  pw: nch floats of workspace.
+mdt_status channel_scales(const float2 *XB, int ne, int nch, int nsp, float target_rms, float *pw,
+                          float *scales, cudaStream_t stream)
+{
+    channel_power_kernel<<<nch, 256, 0, stream>>>(XB, ne, (nsp + 7) / 8, nsp, pw);
+    mdt_status st = launch_status("channel_power_kernel");
+    if (st != MDT_SUCCESS) return st;
+    scales_from_power_kernel<<<(unsigned)cdiv(nch, 256), 256, 0, stream>>>(pw, nch, target_rms,
+                                                                           scales);
+    return launch_status("scales_from_power_kernel");
+}
+
+// Exact-int8 F-engine: X16 layout holding integers in [-127, 127] (f16),
+// requantised per channel with qscales.
+mdt_status fengine_q8(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
+                      const int8_t *iq, const float *win, void *X16, int nep, int nkc,
+                      const float *qscales, cudaStream_t stream)
+{
+    if (((uintptr_t)iq | (uintptr_t)hist | (uintptr_t)win | (uintptr_t)X16) & 15)
+        return invalid("fengine_q8: buffers must be 16-byte aligned");
+    if (!qscales) return invalid("fengine_q8: null scales");
+    FengArgs a = make_args(ne, ntaps, nsp, hist, nhist, iq, win);
+    Feng16Run<__half> run{a, (uint8_t *)X16, nep, nkc, 1.0f, stream};
+    run.qscales = qscales;
+    return dispatch_block8(nch, ntaps, run);
 }
 
 // FP32 F-engine into the 8-spectrum blocked layout XB (fengine_c64b_kernel).
@@ -570,6 +644,18 @@ extern "C" MDT_API mdt_status mdt_fengine_x16(int ne, int nch, int ntaps, int ns
     const int nep = (ne + 15) / 16 * 16, nkc = (nsp + 31) / 32;
     return mdt::fengine_x16(ne, nch, ntaps, nsp, nullptr, 0, iq, window, X16, nep, nkc, ab_fmt,
                             scale, stream);
+}
+
+extern "C" MDT_API mdt_status mdt_fengine_q8(int ne, int nch, int ntaps, int nsp,
+                                             const int8_t *iq, const float *window, void *X16,
+                                             const float *qscales, cudaStream_t stream)
+{
+    mdt_status st = mdt::check_dims(ne, nch, ntaps, nsp);
+    if (st != MDT_SUCCESS) return st;
+    if (!iq || !window || !X16 || !qscales) return mdt::invalid("fengine_q8: null pointer");
+    const int nep = (ne + 15) / 16 * 16, nkc = (nsp + 31) / 32;
+    return mdt::fengine_q8(ne, nch, ntaps, nsp, nullptr, 0, iq, window, X16, nep, nkc, qscales,
+                           stream);
 }
 
 extern "C" MDT_API mdt_status mdt_fengine_c64b(int ne, int nch, int ntaps, int nsp,

@@ -29,6 +29,13 @@ mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, flo
                       float2 *V, double2 *Vacc, int *err, cudaStream_t stream);
 int x16_padded_rows(int ne);
 int x16_chunks(int nsp);
+mdt_status fengine_q8(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
+                      const int8_t *iq, const float *win, void *X16, int nep, int nkc,
+                      const float *qscales, cudaStream_t stream);
+mdt_status xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qscales, float2 *V,
+                      double2 *Vacc, int2 *raw, int *err, cudaStream_t stream);
+mdt_status channel_scales(const float2 *XB, int ne, int nch, int nsp, float target_rms, float *pw,
+                          float *scales, cudaStream_t stream);
 
 // Vacc[i] += V[i] (complex64 -> complex128), the cross-integration sum of the
 // FP32 path.
@@ -55,6 +62,11 @@ struct mdt_fx_plan_s {
     float scale = 1.0f;        // power-of-two F-output scale of the f16/bf16 path
     int *err = nullptr;        // device flag set by a timed-out wait
     double2 *acc = nullptr;    // optional FP64 cross-integration accumulator
+    // exact int8 path: per-channel requantisation scales, calibrated from the
+    // first integration's first spectra unless set by the caller
+    float *qscales = nullptr, *qpower = nullptr;
+    float2 *calib = nullptr;   // FP32 F-output of the calibration spectra
+    bool qscales_valid = false;
     int8_t *hist[2] = {nullptr, nullptr};  // PFB history (double-buffered)
     int cur = 0;
     bool streaming = false;
@@ -82,6 +94,9 @@ void release(mdt_fx_plan p)
     cudaFree(p->X);
     cudaFree(p->X16);
     cudaFree(p->err);
+    cudaFree(p->qscales);
+    cudaFree(p->qpower);
+    cudaFree(p->calib);
     cudaFree(p->hist[0]);
     cudaFree(p->hist[1]);
     for (int i = 0; i < 2; i++) {
@@ -156,6 +171,25 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
                                          256, 0, p->stream>>>((const float2 *)vis, p->acc, n);
             st = mdt::launch_status("accumulate_f64_kernel");
         }
+    } else if (d.precision == MDT_PREC_INT8) {
+        if (!p->qscales_valid) {
+            // calibration: FP32 F-engine over the first spectra of this
+            // integration, scale[c] = 20 / rms_c (int8 clips at 6.3 sigma)
+            const int ncal = std::min(d.nspectra, 64);
+            st = mdt::fengine_c64b(d.nelements, d.nchannels, d.ntaps, ncal, hist, nhist, iq,
+                                   p->window, p->calib, p->stream);
+            if (st == MDT_SUCCESS)
+                st = mdt::channel_scales(p->calib, d.nelements, d.nchannels, ncal, 20.0f,
+                                         p->qpower, p->qscales, p->stream);
+            if (st != MDT_SUCCESS) return st;
+            p->qscales_valid = true;
+        }
+        st = mdt::fengine_q8(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                             p->window, p->X16, p->nep, p->nkc, p->qscales, p->stream);
+        if (st != MDT_SUCCESS) return st;
+        if (t1) cudaEventRecord(t1, p->stream);
+        st = mdt::xengine_q8(d.nelements, d.nchannels, d.nspectra, p->X16, p->qscales,
+                             (float2 *)vis, p->acc, nullptr, p->err, p->stream);
     } else {
         const int fmt = (d.precision == MDT_PREC_BF16) ? 1 : 0;
         st = mdt::fengine_x16(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
@@ -181,7 +215,7 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
                                     desc->nspectra);
     if (st != MDT_SUCCESS) return st;
     if (desc->precision != MDT_PREC_FP32 && desc->precision != MDT_PREC_FP16 &&
-        desc->precision != MDT_PREC_BF16) {
+        desc->precision != MDT_PREC_BF16 && desc->precision != MDT_PREC_INT8) {
         mdt::set_error("fx_create: precision not supported by this build");
         return MDT_ERR_NOT_SUPPORTED;
     }
@@ -208,6 +242,13 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
         if (e == cudaSuccess) e = cudaMalloc(&p->X16, xbytes);
         // padding rows (elements NE..NEp-1) are never written: zero them once
         if (e == cudaSuccess) e = cudaMemset(p->X16, 0, xbytes);
+        if (d.precision == MDT_PREC_INT8) {
+            const size_t cal = sizeof(float2) * (size_t)d.nchannels * 64 * d.nelements;
+            if (e == cudaSuccess) e = cudaMalloc(&p->qscales, sizeof(float) * d.nchannels);
+            if (e == cudaSuccess) e = cudaMalloc(&p->qpower, sizeof(float) * d.nchannels);
+            if (e == cudaSuccess) e = cudaMalloc(&p->calib, cal);
+            xbytes += cal + 2 * sizeof(float) * d.nchannels;
+        }
     }
     if (e == cudaSuccess) e = cudaMalloc(&p->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(p->err, 0, sizeof(int));
@@ -249,7 +290,7 @@ MDT_API mdt_status mdt_fx_set_window(mdt_fx_plan plan, const float *window)
                                                      cudaMemcpyDeviceToDevice, plan->stream),
                                      "fx_set_window");
     if (st != MDT_SUCCESS) return st;
-    if (plan->d.precision != MDT_PREC_FP32) {
+    if (plan->d.precision == MDT_PREC_FP16 || plan->d.precision == MDT_PREC_BF16) {
         // F-output bound for int8 samples: |X| <= 127 sqrt(2) sum |W|; the
         // f16 scale is the power of two that keeps that bound under 60000.
         std::vector<float> h(n);
@@ -274,6 +315,38 @@ MDT_API mdt_status mdt_fx_set_accumulator(mdt_fx_plan plan, void *acc)
     if (((uintptr_t)acc & 15) != 0) return mdt::invalid("fx_set_accumulator: misaligned buffer");
     plan->acc = (double2 *)acc;
     return MDT_SUCCESS;
+}
+
+MDT_API mdt_status mdt_fx_set_channel_scales(mdt_fx_plan plan, const float *scales)
+{
+    if (!plan) return mdt::invalid("fx_set_channel_scales: null plan");
+    if (plan->d.precision != MDT_PREC_INT8) {
+        mdt::set_error("fx_set_channel_scales: plan precision is not INT8");
+        return MDT_ERR_STATE;
+    }
+    if (!scales) {  // recalibrate at the next integration
+        plan->qscales_valid = false;
+        return MDT_SUCCESS;
+    }
+    mdt_status st = mdt::cuda_status(
+        cudaMemcpyAsync(plan->qscales, scales, sizeof(float) * plan->d.nchannels,
+                        cudaMemcpyDeviceToDevice, plan->stream),
+        "fx_set_channel_scales");
+    if (st == MDT_SUCCESS) plan->qscales_valid = true;
+    return st;
+}
+
+MDT_API mdt_status mdt_fx_get_channel_scales(mdt_fx_plan plan, float *scales)
+{
+    if (!plan || !scales) return mdt::invalid("fx_get_channel_scales: null argument");
+    if (plan->d.precision != MDT_PREC_INT8 || !plan->qscales_valid) {
+        mdt::set_error("fx_get_channel_scales: no INT8 scales yet");
+        return MDT_ERR_STATE;
+    }
+    return mdt::cuda_status(cudaMemcpyAsync(scales, plan->qscales,
+                                            sizeof(float) * plan->d.nchannels,
+                                            cudaMemcpyDeviceToDevice, plan->stream),
+                            "fx_get_channel_scales");
 }
 
 MDT_API mdt_status mdt_fx_get_scale(mdt_fx_plan plan, float *scale)

@@ -23,6 +23,18 @@
 // mirror (full square, column-major, the cuBLAS C layout) and can add the
 // result into an FP64 cross-integration accumulator.
 //
+// Exact int8 mode (KIND 1): the F-engine requantises each channel to
+// integers in [-127, 127] (stored as f16, which holds them exactly); the
+// products are exact and an FP32 accumulator stays exact while every partial
+// sum is an integer below 2^24, i.e. for 16 K-chunks (512 spectra:
+// 512 * 2 * 127^2 < 2^24).  The MMAs therefore accumulate one 512-spectrum
+// window at a time into one of two TMEM window buffers; the epilogue warps
+// fold each finished window into int32 running sums kept in TMEM
+// (tcgen05.ld / tcgen05.st) while the MMAs fill the other buffer, and write
+// the exact int32 visibilities (and their scaled float values) at the end.
+// Column chunks are <= 64 wide: 2 windows x (Re, Im) + running (Re, Im) =
+// 6N <= 384 TMEM columns.
+//
 // Warp roles (192 threads): warp 0 lane 0 issues bulk copies into a 4-stage
 // shared-memory ring; warp 1 allocates tensor memory and its lane 0 issues
 // the MMAs and commits; warps 2-5 read the accumulators (one TMEM lane
@@ -58,27 +70,38 @@ struct TcArgs {
     float2 *V;          // [nch][ne*ne] complex64, column-major per channel (may be null)
     double2 *Vacc;      // [nch][ne*ne] complex128 accumulator (may be null)
     int *err;           // set to 1 on a wait timeout
+    const float *qscales;  // exact int8 mode: per-channel requantisation scales
+    int2 *raw;          // exact int8 mode: optional int32 (re, im) visibilities [nch][ne*ne]
     TcTile tiles[TC_MAX_TILES];
 };
 
+constexpr int TC_WIN = 16;  // K-chunks (of 32 spectra) per exact accumulation window
+
+template <int KIND>  // 0: f16 / bf16 operands, float results; 1: exact int8-valued f16
 __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_constant__ TcArgs a)
 {
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + (size_t)TC_STAGES * TC_STAGE_BYTES);
-    // bars[0..S) full, bars[S..2S) empty, bars[2S] done; then the TMEM address slot
-    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 1);
+    // bars[0..S) full, bars[S..2S) empty, bars[2S] done, bars[2S+1..2S+2] window
+    // full, bars[2S+3..2S+4] window empty; then the TMEM address slot
+    uint64_t *win_full = bars + 2 * TC_STAGES + 1;
+    uint64_t *win_empty = bars + 2 * TC_STAGES + 3;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 5);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = blockIdx.x / a.ntiles;
     const TcTile tile = a.tiles[blockIdx.x - ch * a.ntiles];
     const int N = tile.n;
-    const uint32_t ncols = (2 * N <= 32) ? 32 : (2 * N <= 64) ? 64 : (2 * N <= 128) ? 128
-                                                                   : (2 * N <= 256) ? 256 : 512;
+    constexpr int NCOLMUL = (KIND == 0) ? 2 : 6;  // TMEM columns per output column
+    const uint32_t ncols = (NCOLMUL * N <= 32) ? 32 : (NCOLMUL * N <= 64) ? 64
+                         : (NCOLMUL * N <= 128) ? 128 : (NCOLMUL * N <= 256) ? 256 : 512;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < 2 * TC_STAGES + 1; s++) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
+        for (int s = 0; s < 2 * TC_STAGES + 3; s++) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
+        tc::mbar_init(tc::smem_u32(&win_empty[0]), 4);  // one arrival per epilogue warp
+        tc::mbar_init(tc::smem_u32(&win_empty[1]), 4);
         tc::fence_mbar_init();
     }
     if (warp == 1) {
@@ -128,6 +151,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
         const uint32_t id_neg = tc::idesc_f16(N, a.ab_fmt, 1);
         for (int kc = 0; kc < a.nkc && ok; kc++) {
             const int s = kc % TC_STAGES;
+            uint32_t acc_re = d_re, acc_im = d_im;
+            bool first = (kc == 0);
+            if constexpr (KIND == 1) {
+                const int w = kc / TC_WIN, h = w & 1;
+                first = (kc % TC_WIN) == 0;
+                if (first && w >= 2) {  // window buffer h must have been folded (window w-2)
+                    ok = tc::mbar_wait(tc::smem_u32(&win_empty[h]), ((w >> 1) - 1) & 1);
+                    if (!ok) break;
+                    tc::fence_after_sync();
+                }
+                acc_re = tmem + (uint32_t)(h * 2 * N);
+                acc_im = acc_re + (uint32_t)N;
+            }
             ok = tc::mbar_wait(tc::smem_u32(&bars[s]), (kc / TC_STAGES) & 1);
             if (!ok) break;
             tc::fence_after_sync();
@@ -135,21 +171,96 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
             const uint32_t sa = tile.a_sep ? sb + TC_B_BYTES : sb + (uint32_t)(tile.r0 - tile.q0) * 128;
             const uint64_t bd = tc::sw128_kmajor_desc(sb);
             const uint64_t ad = tc::sw128_kmajor_desc(sa);
-            const uint32_t first = (kc == 0);
             // k-step j advances the start address by 32 bytes (+2 in the >>4 field)
-            tc::mma_f16(d_re, ad + 0, bd + 0, id_pos, !first);
-            tc::mma_f16(d_re, ad + 2, bd + 2, id_pos, 1);
-            tc::mma_f16(d_re, ad + 4, bd + 4, id_pos, 1);
-            tc::mma_f16(d_re, ad + 6, bd + 6, id_pos, 1);
-            tc::mma_f16(d_im, ad + 4, bd + 0, id_pos, !first);
-            tc::mma_f16(d_im, ad + 6, bd + 2, id_pos, 1);
-            tc::mma_f16(d_im, ad + 0, bd + 4, id_neg, 1);
-            tc::mma_f16(d_im, ad + 2, bd + 6, id_neg, 1);
+            tc::mma_f16(acc_re, ad + 0, bd + 0, id_pos, !first);
+            tc::mma_f16(acc_re, ad + 2, bd + 2, id_pos, 1);
+            tc::mma_f16(acc_re, ad + 4, bd + 4, id_pos, 1);
+            tc::mma_f16(acc_re, ad + 6, bd + 6, id_pos, 1);
+            tc::mma_f16(acc_im, ad + 4, bd + 0, id_pos, !first);
+            tc::mma_f16(acc_im, ad + 6, bd + 2, id_pos, 1);
+            tc::mma_f16(acc_im, ad + 0, bd + 4, id_neg, 1);
+            tc::mma_f16(acc_im, ad + 2, bd + 6, id_neg, 1);
             tc::mma_commit(tc::smem_u32(&bars[TC_STAGES + s]));
+            if constexpr (KIND == 1) {
+                if ((kc % TC_WIN) == TC_WIN - 1 || kc == a.nkc - 1)
+                    tc::mma_commit(tc::smem_u32(&win_full[(kc / TC_WIN) & 1]));
+            }
         }
         tc::mma_commit(tc::smem_u32(&bars[2 * TC_STAGES]));
         if (!ok) atomicExch(a.err, 1);
-    } else if (warp >= 2) {
+    } else if (warp >= 2 && KIND == 1) {
+        // ---------------- epilogue, exact int8 mode: fold windows into int32
+        const int quarter = warp & 3;
+        const int r = tile.r0 + quarter * 32 + lane;
+        const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+        const uint32_t run_re = tmem + (uint32_t)(4 * N), run_im = tmem + (uint32_t)(5 * N);
+        const int nwin = (a.nkc + TC_WIN - 1) / TC_WIN;
+        float2 *Vc = a.V ? a.V + (long)ch * a.ne * a.ne : nullptr;
+        double2 *Ac = a.Vacc ? a.Vacc + (long)ch * a.ne * a.ne : nullptr;
+        int2 *Rc = a.raw ? a.raw + (long)ch * a.ne * a.ne : nullptr;
+        const float qs = __ldg(a.qscales + ch);
+        const float alpha = a.alpha / (qs * qs);
+        for (int w = 0; w < nwin; w++) {
+            const int h = w & 1;
+            ok = ok && tc::mbar_wait_sleep(tc::smem_u32(&win_full[h]), (w >> 1) & 1);
+            tc::fence_after_sync();
+            const uint32_t wre = tmem + (uint32_t)(h * 2 * N), wim = wre + (uint32_t)N;
+            const bool last = (w == nwin - 1);
+            for (int n0 = 0; n0 < N; n0 += 16) {
+                uint32_t vr[16], vi[16], rr[16], ri[16];
+                tc::tmem_ld16(wre + lane_off + n0, vr);
+                tc::tmem_ld16(wim + lane_off + n0, vi);
+                if (w > 0) {
+                    tc::tmem_ld16(run_re + lane_off + n0, rr);
+                    tc::tmem_ld16(run_im + lane_off + n0, ri);
+                }
+                tc::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    // the window sums are integers below 2^24: exact in FP32
+                    const int xr = __float2int_rn(__uint_as_float(vr[j]));
+                    const int xi = __float2int_rn(__uint_as_float(vi[j]));
+                    rr[j] = (uint32_t)((w > 0 ? (int)rr[j] : 0) + xr);
+                    ri[j] = (uint32_t)((w > 0 ? (int)ri[j] : 0) + xi);
+                }
+                if (!last) {
+                    tc::tmem_st16(run_re + lane_off + n0, rr);
+                    tc::tmem_st16(run_im + lane_off + n0, ri);
+                } else if (ok && r < a.ne) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const int q = tile.q0 + n0 + j;
+                        if (q >= a.ne || q > r) continue;
+                        const int ire = (int)rr[j];
+                        const int iim = (q == r) ? 0 : (int)ri[j];
+                        const long lo = (long)q * a.ne + r, up = (long)r * a.ne + q;
+                        if (Rc) {
+                            Rc[lo] = make_int2(ire, iim);
+                            if (q != r) Rc[up] = make_int2(ire, -iim);
+                        }
+                        const float re = (float)ire * alpha, im = (float)iim * alpha;
+                        if (Vc) {
+                            Vc[lo] = make_float2(re, im);
+                            if (q != r) Vc[up] = make_float2(re, -im);
+                        }
+                        if (Ac) {
+                            double2 x = Ac[lo];
+                            Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
+                            if (q != r) {
+                                double2 y = Ac[up];
+                                Ac[up] = make_double2(y.x + (double)re, y.y - (double)im);
+                            }
+                        }
+                    }
+                }
+            }
+            if (!last) tc::tmem_st_wait();
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&win_empty[h]));
+        }
+        if (!ok && lane == 0) atomicExch(a.err, 1);
+    } else if (warp >= 2 && KIND == 0) {
         // ---------------- epilogue: TMEM -> visibilities
         ok = tc::mbar_wait_sleep(tc::smem_u32(&bars[2 * TC_STAGES]), 0);
         tc::fence_after_sync();
@@ -197,22 +308,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
 
 // Lower-triangle work list for NE elements: row tiles of 128, column chunks
 // of up to 256 from 0 to the end of the row tile's diagonal block.
-static int make_tiles(int ne, int nep, TcTile *tiles)
+static int make_tiles(int ne, int nep, int maxw, TcTile *tiles)
 {
     int n = 0;
     for (int r0 = 0; r0 < nep; r0 += TC_AROWS) {
         const int cend = std::min(nep, r0 + TC_AROWS);
-        for (int q0 = 0; q0 < cend; q0 += TC_BROWS) {
+        for (int q0 = 0; q0 < cend; q0 += maxw) {
             if (n >= TC_MAX_TILES) return -1;
-            const int w = std::min(TC_BROWS, cend - q0);
+            const int w = std::min(maxw, cend - q0);
             TcTile t;
             t.r0 = (int16_t)r0;
             t.q0 = (int16_t)q0;
             t.n = (int16_t)w;
-            // A inside the loaded B rows iff the chunk covers rows r0..r0+127
-            // (rows past NEp read stale shared memory and only feed
-            // accumulator rows that are never stored)
-            t.a_sep = (int16_t)(q0 + w <= r0 ? 1 : 0);
+            // A is read from the B rows only when the chunk holds every valid
+            // row of the tile (rows past NEp feed accumulator rows that are
+            // never stored) and the 128 A rows stay inside the B region of
+            // the stage; otherwise A is loaded on its own.
+            const bool inside = q0 <= r0 && std::min(r0 + TC_AROWS, nep) <= q0 + w &&
+                                r0 - q0 + TC_AROWS <= TC_BROWS;
+            t.a_sep = (int16_t)(inside ? 0 : 1);
             tiles[n++] = t;
         }
     }
@@ -239,18 +353,63 @@ mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, flo
     a.V = V;
     a.Vacc = Vacc;
     a.err = err;
-    a.ntiles = make_tiles(ne, a.nep, a.tiles);
+    a.qscales = nullptr;
+    a.raw = nullptr;
+    a.ntiles = make_tiles(ne, a.nep, TC_BROWS, a.tiles);
     if (a.ntiles <= 0) return invalid("xengine_tc: too many tiles");
-    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel,
+    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<0>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
     if (e != cudaSuccess) return cuda_status(e, "xengine_tc smem attribute");
     long blocks = (long)nch * a.ntiles;
     if (blocks > 0x7fffffffL) return invalid("xengine_tc: grid too large");
-    xengine_tc_kernel<<<(unsigned)blocks, TC_THREADS, TC_SMEM, stream>>>(a);
+    xengine_tc_kernel<0><<<(unsigned)blocks, TC_THREADS, TC_SMEM, stream>>>(a);
     return launch_status("xengine_tc_kernel");
 }
 
+// Exact int8 mode: X16 holds integers in [-127, 127] (f16) requantised with
+// qscales[c]; vis = int32 sums / (Nsp * qscales[c]^2); raw = the int32 sums.
+mdt_status xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qscales, float2 *V,
+                      double2 *Vacc, int2 *raw, int *err, cudaStream_t stream)
+{
+    if (!X16 || !qscales || (!V && !Vacc && !raw) || !err)
+        return invalid("xengine_q8: null pointer");
+    if (((uintptr_t)X16 & 15) != 0) return invalid("xengine_q8: X16 must be 16-byte aligned");
+    TcArgs a;
+    a.ne = ne;
+    a.nep = x16_padded_rows(ne);
+    a.nkc = x16_chunks(nsp);
+    a.chunk_bytes = (long)a.nep * 128;
+    a.chan_bytes = (long)a.nkc * a.chunk_bytes;
+    a.X = (const uint8_t *)X16;
+    a.ab_fmt = 0;
+    a.alpha = 1.0f / (float)nsp;
+    a.V = V;
+    a.Vacc = Vacc;
+    a.err = err;
+    a.qscales = qscales;
+    a.raw = raw;
+    a.ntiles = make_tiles(ne, a.nep, 64, a.tiles);
+    if (a.ntiles <= 0) return invalid("xengine_q8: too many tiles");
+    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "xengine_q8 smem attribute");
+    long blocks = (long)nch * a.ntiles;
+    if (blocks > 0x7fffffffL) return invalid("xengine_q8: grid too large");
+    xengine_tc_kernel<1><<<(unsigned)blocks, TC_THREADS, TC_SMEM, stream>>>(a);
+    return launch_status("xengine_tc_kernel<exact int8>");
+}
+
 }  // namespace mdt
+
+extern "C" MDT_API mdt_status mdt_xengine_q8(int ne, int nch, int nsp, const void *X16,
+                                             const float *qscales, void *vis, void *vis_acc,
+                                             void *vis_i32, int *err, cudaStream_t stream)
+{
+    if (ne < 1 || ne > MDT_MAX_ELEMENTS || nch < 1 || nsp < 1 || nsp > MDT_MAX_SPECTRA)
+        return mdt::invalid("xengine_q8: bad arguments");
+    return mdt::xengine_q8(ne, nch, nsp, X16, qscales, (float2 *)vis, (double2 *)vis_acc,
+                           (int2 *)vis_i32, err, stream);
+}
 
 extern "C" MDT_API mdt_status mdt_xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt,
                                              float scale, void *vis, void *vis_acc, int *err,
