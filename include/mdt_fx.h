@@ -288,6 +288,40 @@ MDT_API mdt_status mdt_fx_get_timing(mdt_fx_plan plan, double *fengine_ms, doubl
                                      int *count);
 
 /* ------------------------------------------------------------------------
+ * 4. Batches: many independent jobs of uneven shape (survey configuration
+ *    "24 ragged jobs"), f16 tensor-core path, Nch <= 2048, Ntaps 4 or 8.
+ *    One F-engine launch per (Nch, Ntaps) group and one persistent X-engine
+ *    launch over a work list spanning every job, captured in a CUDA graph on
+ *    the batch's own stream and replayed; the X-engine's column-chunk width
+ *    and work order come from an autotuner (timed on the batch, cached per
+ *    shape; also in the file named by MDT_AUTOTUNE_CACHE when set).
+ * ---------------------------------------------------------------------- */
+typedef struct mdt_fx_batch_s *mdt_fx_batch;
+
+/* descs[j]: each job's shape (precision must be MDT_PREC_FP16).  Allocates the
+ * jobs' F-output buffers and a non-blocking stream; windows default to the
+ * Hamming windowed sinc (mdt_window_hamming_sinc). */
+MDT_API mdt_status mdt_fx_batch_create(const mdt_fx_desc *descs, int njobs, mdt_fx_batch *batch);
+MDT_API mdt_status mdt_fx_batch_destroy(mdt_fx_batch batch);
+/* Replaces job's window (device, Ntaps*Nch floats). */
+MDT_API mdt_status mdt_fx_batch_set_window(mdt_fx_batch batch, int job, const float *window);
+/* The stream every batch launch is issued on (synchronise on it or use
+ * mdt_fx_batch_check). */
+MDT_API mdt_status mdt_fx_batch_get_stream(mdt_fx_batch batch, cudaStream_t *stream);
+/* Runs the autotuner now (otherwise the first execute does); reports the
+ * chosen column-chunk width and whether the work list is cost-ordered. */
+MDT_API mdt_status mdt_fx_batch_autotune(mdt_fx_batch batch, int *maxw, int *cost_order);
+/* One integration of every job: iq[j] (device, Nsp_j + Ntaps_j - 1 spectra,
+ * 16-byte aligned) -> vis[j] (device, complex64 [Nch_j][NE_j*NE_j]); iq and
+ * vis are host arrays of njobs device pointers.  use_graph = 1 replays the
+ * captured graph (captured on first use), 0 launches the kernels directly.
+ * Asynchronous on the batch's stream. */
+MDT_API mdt_status mdt_fx_batch_execute(mdt_fx_batch batch, const int8_t *const *iq,
+                                        void *const *vis, int use_graph);
+/* Waits for the batch's stream; MDT_ERR_TIMEOUT if a bounded device wait gave up. */
+MDT_API mdt_status mdt_fx_batch_check(mdt_fx_batch batch);
+
+/* ------------------------------------------------------------------------
  * One integration without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory
  * themselves -- a real-time ingest loop in which cudaMalloc's implicit device

@@ -24,7 +24,7 @@ from .binding import (  # noqa: F401
     CUFFT_FORWARD, CUFFT_INVERSE, CUFFT_C2C, CUBLAS_OP_N, CUBLAS_OP_T, CUBLAS_OP_C,
     window_hamming_sinc, fft_c2c, xengine_f32, fengine_f32, synth_iq,
     fengine_x16, xengine_tc, x16_bytes, fengine_c64b, fx_integrate_static,
-    FxPlan, MDT_PREC_FP32, MDT_PREC_FP16, MDT_PREC_BF16, MDT_PREC_INT8,
+    FxPlan, FxBatch, MDT_PREC_FP32, MDT_PREC_FP16, MDT_PREC_BF16, MDT_PREC_INT8,
     fengine_q8, xengine_q8,
 )
 from . import configs  # noqa: F401

@@ -79,6 +79,13 @@ def _declare(L):
         "mdt_fx_set_timing": ([_P, _I], _I),
         "mdt_fx_get_timing": ([_P, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)], _I),
+        "mdt_fx_batch_create": ([_P, _I, ctypes.POINTER(_P)], _I),
+        "mdt_fx_batch_destroy": ([_P], _I),
+        "mdt_fx_batch_set_window": ([_P, _I, _P], _I),
+        "mdt_fx_batch_get_stream": ([_P, ctypes.POINTER(_P)], _I),
+        "mdt_fx_batch_autotune": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+        "mdt_fx_batch_execute": ([_P, _P, _P, _I], _I),
+        "mdt_fx_batch_check": ([_P], _I),
         "cufftPlan1d": ([ctypes.POINTER(_I), _I, _I, _I], _I),
         "cufftSetStream": ([_I, _P], _I),
         "cufftExecC2C": ([_I, _P, _P, _I], _I),
@@ -376,6 +383,55 @@ class FxPlan:
     def close(self):
         if self._h:
             check(lib().mdt_fx_destroy(self._h), "mdt_fx_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class FxBatch:
+    """Many independent jobs (mdt_fx_batch_*): jobs = [(NE, Nch, Ntaps, Nsp), ...],
+    f16 tensor-core path, one graph-captured batch launch per integration."""
+
+    def __init__(self, jobs):
+        self.jobs = [tuple(int(v) for v in j) for j in jobs]
+        arr = (_Desc * len(self.jobs))(*[_Desc(ne, nch, nt, nsp, MDT_PREC_FP16)
+                                         for ne, nch, nt, nsp in self.jobs])
+        h = _P()
+        check(lib().mdt_fx_batch_create(arr, len(self.jobs), ctypes.byref(h)), "mdt_fx_batch_create")
+        self._h = h
+
+    @property
+    def stream(self):
+        s = _P()
+        check(lib().mdt_fx_batch_get_stream(self._h, ctypes.byref(s)), "mdt_fx_batch_get_stream")
+        return s.value
+
+    def set_window(self, job, window):
+        check(lib().mdt_fx_batch_set_window(self._h, job, ptr(window)), "mdt_fx_batch_set_window")
+
+    def autotune(self):
+        w, o = _I(0), _I(0)
+        check(lib().mdt_fx_batch_autotune(self._h, ctypes.byref(w), ctypes.byref(o)),
+              "mdt_fx_batch_autotune")
+        return w.value, bool(o.value)
+
+    def execute(self, iqs, viss, use_graph=True):
+        n = len(self.jobs)
+        a = (_P * n)(*[ptr(x) for x in iqs])
+        b = (_P * n)(*[ptr(x) for x in viss])
+        check(lib().mdt_fx_batch_execute(self._h, a, b, 1 if use_graph else 0),
+              "mdt_fx_batch_execute")
+
+    def check(self):
+        check(lib().mdt_fx_batch_check(self._h), "mdt_fx_batch_check")
+
+    def close(self):
+        if self._h:
+            check(lib().mdt_fx_batch_destroy(self._h), "mdt_fx_batch_destroy")
             self._h = None
 
     def __del__(self):

@@ -19,6 +19,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include "fengine.cuh"
 #include "fft_core.cuh"
 
 namespace mdt {
@@ -250,17 +251,18 @@ __device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, in
     }
 }
 
-// Block decode: blockIdx.x = (kc * NE + e) * 4 + jsub, s0 = 32 kc + 8 jsub.
+// Block decode: blk = (kc * NE + e) * 4 + jsub, s0 = 32 kc + 8 jsub.
 struct Block8 {
     int jsub, e, kc, s0;
-    __device__ __forceinline__ explicit Block8(int ne)
+    __device__ __forceinline__ Block8(int ne, int blk)
     {
-        jsub = blockIdx.x & 3;
-        const int rest = blockIdx.x >> 2;
+        jsub = blk & 3;
+        const int rest = blk >> 2;
         e = rest % ne;
         kc = rest / ne;
         s0 = kc * 32 + jsub * 8;
     }
+    __device__ __forceinline__ explicit Block8(int ne) : Block8(ne, (int)blockIdx.x) {}
 };
 
 // Tap sum + FFT of the block's 8 rows; the spectra stay in shared memory
@@ -367,6 +369,56 @@ __global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
         uim.y = pack2<H>(prep<QUANT>(v[2].y, sc), prep<QUANT>(v[3].y, sc));
         uim.z = pack2<H>(prep<QUANT>(v[4].y, sc), prep<QUANT>(v[5].y, sc));
         uim.w = pack2<H>(prep<QUANT>(v[6].y, sc), prep<QUANT>(v[7].y, sc));
+        uint8_t *row = rowbase + (size_t)c * cstride;
+        *reinterpret_cast<uint4 *>(row + pre) = ure;
+        *reinterpret_cast<uint4 *>(row + pim) = uim;
+    }
+}
+
+// ------------------------------------------------------------------------
+// Batched f16 F-engine: one launch for every job of a batch that shares
+// (Nch, Ntaps).  Job j owns blocks [blk0[j], blk0[j+1]); within a job the
+// blocks decode as in fengine_x16_kernel.
+template <int N, int NT>
+__global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
+    fengine_x16_batched_kernel(const FJob *__restrict__ jobs, int njobs, const float2 *tw)
+{
+    using C = FengBCfg<N>;
+    extern __shared__ float2 fsm[];
+    int j = 0;
+    while (j + 1 < njobs && (int)blockIdx.x >= jobs[j + 1].blk0) j++;
+    const FJob jb = jobs[j];
+    FengArgs a;
+    a.hist = nullptr;
+    a.iq = jb.iq;
+    a.nhist = 0;
+    a.ne = jb.ne;
+    a.ntaps = NT;
+    a.nsp = jb.nsp;
+    a.ngroups = 0;
+    a.win = jb.win;
+    a.tw = tw;
+    a.X = nullptr;
+    const Block8 b(jb.ne, (int)blockIdx.x - jb.blk0);
+    fengine_block8<N, NT>(a, b, fsm);
+
+    uint8_t *rowbase = jb.X16 + ((size_t)b.kc * jb.nep + b.e) * 128;
+    const size_t cstride = (size_t)jb.nkc * jb.nep * 128;
+    const int pre = (b.jsub ^ (b.e & 7)) << 4, pim = ((4 + b.jsub) ^ (b.e & 7)) << 4;
+    const float sc = jb.scale;
+    for (int c = threadIdx.x; c < N; c += C::THREADS) {
+        float2 v[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) v[r] = fsm[(size_t)r * C::RSTRIDE + fft::pad(c)];
+        uint4 ure, uim;
+        ure.x = pack2<__half>(v[0].x * sc, v[1].x * sc);
+        ure.y = pack2<__half>(v[2].x * sc, v[3].x * sc);
+        ure.z = pack2<__half>(v[4].x * sc, v[5].x * sc);
+        ure.w = pack2<__half>(v[6].x * sc, v[7].x * sc);
+        uim.x = pack2<__half>(v[0].y * sc, v[1].y * sc);
+        uim.y = pack2<__half>(v[2].y * sc, v[3].y * sc);
+        uim.z = pack2<__half>(v[4].y * sc, v[5].y * sc);
+        uim.w = pack2<__half>(v[6].y * sc, v[7].y * sc);
         uint8_t *row = rowbase + (size_t)c * cstride;
         *reinterpret_cast<uint4 *>(row + pre) = ure;
         *reinterpret_cast<uint4 *>(row + pim) = uim;
@@ -512,6 +564,41 @@ mdt_status fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *hist, 
         return dispatch_block8(nch, ntaps,
                                Feng16Run<__nv_bfloat16>{a, (uint8_t *)X16, nep, nkc, scale, stream});
     return dispatch_block8(nch, ntaps, Feng16Run<__half>{a, (uint8_t *)X16, nep, nkc, scale, stream});
+}
+
+struct FengBatchRun {
+    const FJob *jobs;
+    int njobs;
+    long nblocks;
+    cudaStream_t stream;
+    template <int N, int NT>
+    mdt_status run()
+    {
+        if constexpr (NT == 0) {
+            return invalid("batched F-engine: Ntaps must be 4 or 8");
+        } else {
+            using C = FengBCfg<N>;
+            mdt_status st;
+            const float2 *tw = fft_twiddles(N, &st);
+            if (!tw) return st;
+            cudaError_t e = cudaFuncSetAttribute(fengine_x16_batched_kernel<N, NT>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)C::SMEM);
+            if (e != cudaSuccess) return cuda_status(e, "batched F-engine smem attribute");
+            if (nblocks > 0x7fffffffL) return invalid("batched F-engine: grid too large");
+            fengine_x16_batched_kernel<N, NT><<<(unsigned)nblocks, C::THREADS, C::SMEM, stream>>>(
+                jobs, njobs, tw);
+            return launch_status("fengine_x16_batched_kernel");
+        }
+    }
+};
+
+// Batched f16 F-engine launch over jobs sharing (nch, ntaps in {4, 8});
+// `jobs` is a device array of njobs FJob, `nblocks` the total block count.
+mdt_status fengine_x16_batched(int nch, int ntaps, const FJob *jobs, int njobs, long nblocks,
+                               cudaStream_t stream)
+{
+    return dispatch_block8(nch, ntaps, FengBatchRun{jobs, njobs, nblocks, stream});
 }
 
 // Per-channel int8 scales from the power of a blocked FP32 F-output:

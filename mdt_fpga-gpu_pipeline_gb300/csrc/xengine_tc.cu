@@ -42,6 +42,7 @@
 // timeout sets the error flag and the block finishes without further work.
 #include "mdt_common.cuh"
 #include "tc_ptx.cuh"
+#include "xengine_tc.cuh"
 
 namespace mdt {
 
@@ -55,9 +56,6 @@ constexpr uint32_t TC_A_BYTES = TC_AROWS * 128;
 constexpr uint32_t TC_STAGE_BYTES = TC_B_BYTES + TC_A_BYTES;
 constexpr size_t TC_SMEM = 1024 /*align slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES + 256;
 
-struct TcTile {
-    int16_t r0, q0, n, a_sep;  // row-tile start, column-chunk start, chunk width, A loaded apart
-};
 
 struct TcArgs {
     const uint8_t *X;   // X16 operand base
@@ -306,9 +304,168 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
     }
 }
 
+// ------------------------------------------------------------------------
+// Persistent batched X-engine (kind::f16): one launch for every job of a
+// batch.  The work list holds (job, channel, tile) entries, sorted by the
+// host; block b processes entries b, b + grid, b + 2 grid, ...  The shared
+// memory stage ring runs on across entries, and the two TMEM accumulator
+// sets (Re | Im, N <= 128 columns each, at columns 0 and 256) alternate
+// between consecutive entries, so the epilogue of one entry overlaps the
+// MMAs of the next.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    xengine_tc_batched_kernel(const XJob *__restrict__ jobs, const XWork *__restrict__ work,
+                              int nwork, int *err)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + (size_t)TC_STAGES * TC_STAGE_BYTES);
+    uint64_t *acc_full = bars + 2 * TC_STAGES, *acc_empty = bars + 2 * TC_STAGES + 2;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2 * TC_STAGES + 2; s++) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
+        tc::mbar_init(tc::smem_u32(&acc_empty[0]), 4);
+        tc::mbar_init(tc::smem_u32(&acc_empty[1]), 4);
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(tc::smem_u32(tmem_slot), 512);
+        tc::tmem_relinquish();
+        tc::fence_before_sync();
+    }
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    bool ok = true;
+
+    if (warp == 0 && lane == 0) {
+        long it = 0;  // stage-ring position across entries
+        for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+            const XWork wk = work[w];
+            const XJob jb = jobs[wk.job];
+            const uint8_t *xc = jb.X + (long)wk.ch * jb.chan_bytes;
+            const uint32_t bbytes = (uint32_t)wk.tile.n * 128;
+            const int arows = min(TC_AROWS, jb.nep - wk.tile.r0);
+            const uint32_t abytes = wk.tile.a_sep ? (uint32_t)arows * 128 : 0;
+            for (int kc = 0; kc < jb.nkc && ok; kc++, it++) {
+                const int s = (int)(it % TC_STAGES);
+                if (it >= TC_STAGES) {
+                    ok = tc::mbar_wait(tc::smem_u32(&bars[TC_STAGES + s]),
+                                       (uint32_t)((it / TC_STAGES) - 1) & 1);
+                    if (!ok) break;
+                }
+                uint8_t *stage = smem + (size_t)s * TC_STAGE_BYTES;
+                const uint32_t full = tc::smem_u32(&bars[s]);
+                tc::mbar_expect_tx(full, bbytes + abytes);
+                const uint8_t *src = xc + (long)kc * jb.chunk_bytes;
+                tc::bulk_g2s(tc::smem_u32(stage), src + (long)wk.tile.q0 * 128, bbytes, full);
+                if (abytes)
+                    tc::bulk_g2s(tc::smem_u32(stage + TC_B_BYTES), src + (long)wk.tile.r0 * 128,
+                                 abytes, full);
+            }
+        }
+        // drain: every issued stage consumed before the block exits
+        for (long k = (it > TC_STAGES ? it - TC_STAGES : 0); k < it && ok; k++)
+            ok = tc::mbar_wait(tc::smem_u32(&bars[TC_STAGES + (int)(k % TC_STAGES)]),
+                               (uint32_t)(k / TC_STAGES) & 1);
+        if (!ok) atomicExch(err, 1);
+    } else if (warp == 1 && lane == 0) {
+        long it = 0;
+        int t = 0;
+        for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x, t++) {
+            const XWork wk = work[w];
+            const XJob jb = jobs[wk.job];
+            const int N = wk.tile.n, h = t & 1;
+            if (t >= 2) {
+                ok = tc::mbar_wait(tc::smem_u32(&acc_empty[h]), ((t >> 1) - 1) & 1);
+                if (!ok) break;
+                tc::fence_after_sync();
+            }
+            const uint32_t d_re = tmem + (uint32_t)(h * 256), d_im = d_re + (uint32_t)N;
+            const uint32_t id_pos = tc::idesc_f16(N, 0, 0), id_neg = tc::idesc_f16(N, 0, 1);
+            for (int kc = 0; kc < jb.nkc && ok; kc++, it++) {
+                const int s = (int)(it % TC_STAGES);
+                ok = tc::mbar_wait(tc::smem_u32(&bars[s]), (uint32_t)(it / TC_STAGES) & 1);
+                if (!ok) break;
+                tc::fence_after_sync();
+                const uint32_t sb = tc::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
+                const uint32_t sa = wk.tile.a_sep ? sb + TC_B_BYTES
+                                                  : sb + (uint32_t)(wk.tile.r0 - wk.tile.q0) * 128;
+                const uint64_t bd = tc::sw128_kmajor_desc(sb), ad = tc::sw128_kmajor_desc(sa);
+                const uint32_t acc = kc > 0;
+                tc::mma_f16(d_re, ad + 0, bd + 0, id_pos, acc);
+                tc::mma_f16(d_re, ad + 2, bd + 2, id_pos, 1);
+                tc::mma_f16(d_re, ad + 4, bd + 4, id_pos, 1);
+                tc::mma_f16(d_re, ad + 6, bd + 6, id_pos, 1);
+                tc::mma_f16(d_im, ad + 4, bd + 0, id_pos, acc);
+                tc::mma_f16(d_im, ad + 6, bd + 2, id_pos, 1);
+                tc::mma_f16(d_im, ad + 0, bd + 4, id_neg, 1);
+                tc::mma_f16(d_im, ad + 2, bd + 6, id_neg, 1);
+                tc::mma_commit(tc::smem_u32(&bars[TC_STAGES + s]));
+            }
+            tc::mma_commit(tc::smem_u32(&acc_full[h]));
+        }
+        if (!ok) atomicExch(err, 1);
+    } else if (warp >= 2) {
+        const int quarter = warp & 3;
+        const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+        int t = 0;
+        for (int w = blockIdx.x; w < nwork; w += gridDim.x, t++) {
+            const XWork wk = work[w];
+            const XJob jb = jobs[wk.job];
+            const int N = wk.tile.n, h = t & 1;
+            ok = ok && tc::mbar_wait_sleep(tc::smem_u32(&acc_full[h]), (t >> 1) & 1);
+            tc::fence_after_sync();
+            const uint32_t d_re = tmem + (uint32_t)(h * 256), d_im = d_re + (uint32_t)N;
+            const int r = wk.tile.r0 + quarter * 32 + lane;
+            // no visibility buffer (autotuning before the first execute): no writes
+            float2 *Vc = jb.V ? jb.V + (long)wk.ch * jb.ne * jb.ne : nullptr;
+            for (int n0 = 0; n0 < N; n0 += 16) {
+                uint32_t vr[16], vi[16];
+                tc::tmem_ld16(d_re + lane_off + n0, vr);
+                tc::tmem_ld16(d_im + lane_off + n0, vi);
+                tc::tmem_ld_wait();
+                if (!ok || r >= jb.ne || !Vc) continue;
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int q = wk.tile.q0 + n0 + j;
+                    if (q >= jb.ne || q > r) continue;
+                    const float re = __uint_as_float(vr[j]) * jb.alpha;
+                    const float im = (q == r) ? 0.0f : __uint_as_float(vi[j]) * jb.alpha;
+                    Vc[(long)q * jb.ne + r] = make_float2(re, im);
+                    if (q != r) Vc[(long)r * jb.ne + q] = make_float2(re, -im);
+                }
+            }
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(tc::smem_u32(&acc_empty[h]));
+            if (!ok) break;
+        }
+        if (!ok && lane == 0) atomicExch(err, 1);
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 512);
+    }
+}
+
+mdt_status xengine_tc_batched(const XJob *jobs, const XWork *work, int nwork, int *err,
+                              cudaStream_t stream)
+{
+    if (nwork <= 0) return MDT_SUCCESS;
+    cudaError_t e = cudaFuncSetAttribute(xengine_tc_batched_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "batched X-engine smem attribute");
+    const int blocks = std::min(nwork, sm_count());
+    xengine_tc_batched_kernel<<<blocks, TC_THREADS, TC_SMEM, stream>>>(jobs, work, nwork, err);
+    return launch_status("xengine_tc_batched_kernel");
+}
+
 // Lower-triangle work list for NE elements: row tiles of 128, column chunks
 // of up to 256 from 0 to the end of the row tile's diagonal block.
-static int make_tiles(int ne, int nep, int maxw, TcTile *tiles)
+int make_tiles(int ne, int nep, int maxw, TcTile *tiles)
 {
     int n = 0;
     for (int r0 = 0; r0 < nep; r0 += TC_AROWS) {
