@@ -267,6 +267,47 @@ def tensor_path_section(mdt, dev, steps):
     }
 
 
+def batch_section(mdt, dev, steps):
+    """Configuration 4: 24 ragged jobs (ragged_jobs()) in one graph-captured
+    batch (f16 tensor path), aggregate antenna-samples/s per graph replay."""
+    import torch
+    jobs = mdt.configs.ragged_jobs()
+    shapes = [(j.nelements, j.nchannels, j.ntaps, j.nspectra) for j in jobs]
+    batch = mdt.FxBatch(shapes)
+    maxw, cost_order = batch.autotune()
+    iqs, viss = [], []
+    for j in jobs:
+        total = j.nspectra + j.ntaps - 1
+        iq = torch.empty(total * j.nelements * j.nchannels * 2, dtype=torch.int8, device=dev)
+        tone = j.tone_q16()
+        mdt.synth_iq(j.seed, j.nelements, j.nchannels, 0, total,
+                     torch.from_numpy(j.sigma_q8()).to(dev), iq,
+                     tone_q16=None if tone is None else torch.from_numpy(tone).to(dev))
+        iqs.append(iq)
+        viss.append(torch.empty(j.nchannels, j.nelements, j.nelements, dtype=torch.complex64,
+                                device=dev))
+    torch.cuda.synchronize()
+    batch.execute(iqs, viss)  # capture + first replay
+    batch.check()
+    stream = torch.cuda.ExternalStream(batch.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        batch.execute(iqs, viss)
+    e1.record(stream)
+    batch.check()
+    ms = e0.elapsed_time(e1) / steps
+    samples = sum(j.antenna_samples() for j in jobs)
+    batch.close()
+    del iqs, viss
+    torch.cuda.empty_cache()
+    return {"workload": "c4_ragged24", "jobs": len(jobs), "value": samples / (ms * 1e-3),
+            "unit": "antenna-samples/s", "ms_per_step": ms, "autotuned_maxw": maxw,
+            "cost_ordered_work": cost_order, "graph": True,
+            "precision": "f16 operands, fp32 accumulate"}
+
+
 def run_ours(args, cfg):
     import torch
     mdt = load_pkg()
@@ -407,6 +448,9 @@ def run_ours(args, cfg):
     tensor = None
     if not args.no_tensor:
         tensor = tensor_path_section(mdt, dev, steps=max(1, min(args.steps, 3)))
+    batched = None
+    if not args.no_batch:
+        batched = batch_section(mdt, dev, steps=max(1, min(args.steps, 5)))
 
     line = None
     if rank == 0:
@@ -433,6 +477,7 @@ def run_ours(args, cfg):
             "cpu_baseline": cpu,
             "clocks": clk,
             "tensor_path": tensor,
+            "batched": batched,
         }
         print(json.dumps(line))
     plan.close()
@@ -452,6 +497,7 @@ def main():
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e run")
+    ap.add_argument("--no-batch", action="store_true", help="skip the c4 ragged-batch section")
     ap.add_argument("--no-tensor", action="store_true",
                     help="skip the c3 tensor-core vs FP32 section")
     ap.add_argument("--precision", choices=["fp32", "fp16", "bf16"], default="fp32",

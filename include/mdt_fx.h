@@ -322,6 +322,48 @@ MDT_API mdt_status mdt_fx_batch_execute(mdt_fx_batch batch, const int8_t *const 
 MDT_API mdt_status mdt_fx_batch_check(mdt_fx_batch batch);
 
 /* ------------------------------------------------------------------------
+ * Adjoints (differentiation through the FX path).  No counterpart in the
+ * reference, which only runs forward; these are the backward halves of
+ * mdt_fengine_f32 -> gains -> mdt_xengine_f32 for gain calibration and PFB
+ * tap optimisation.  Gradients follow PyTorch's convention for complex
+ * values: grad(z) = dL/dRe(z) + i dL/dIm(z) for a real loss L.  All complex
+ * buffers are complex64; all are device pointers.
+ *
+ * Y[c][s][e] = gains[c][e] * X[c][s][e]   (X, Y: the layout of
+ * mdt_fengine_f32; gains complex64 [Nch][NE]). */
+MDT_API mdt_status mdt_apply_gains(int ne, int nch, int nsp, const void *X, const void *gains,
+                                   void *Y, cudaStream_t stream);
+
+/* X-engine adjoint: for V_c = scale * Y_c Y_c^H (mdt_xengine_f32, Y_c =
+ * NE x Nsp, stored Y[c][s][e]) and G = grad(V) in the same column-major
+ * visibility layout (G[c][q*NE + r] = G_rq),
+ *   dY_c = scale * (G_c + G_c^H) Y_c          written dY[c][s][e]. */
+MDT_API mdt_status mdt_xengine_adjoint_f32(int ne, int nch, int nsp, const void *G, const void *Y,
+                                           void *dY, float scale, cudaStream_t stream);
+
+/* Adjoint of the gains and of the channel-major reorder, given dY:
+ *   dgains[c][e] = sum_s dY[c][s][e] conj(X[c][s][e])   (if dgains != NULL;
+ *                  double accumulation, fixed order)
+ *   dF[s][e][c]  = conj(gains[c][e]) dY[c][s][e]         (if dF != NULL;
+ *                  gains NULL means unit gains).
+ * dF is the gradient of the FFT output rows; mdt_fft_c2c with direction +1
+ * (the unnormalised inverse) turns it into the gradient of the PFB output. */
+MDT_API mdt_status mdt_gain_adjoint(int ne, int nch, int nsp, const void *dY, const void *X,
+                                    const void *gains, void *dgains, void *dF,
+                                    cudaStream_t stream);
+
+/* PFB tap gradient: with P[s][e][k] = sum_i W[i*Nch + k] in[s+i][e][k]
+ * (PpS_Batch, reference MDT_device_functions.cu) and gradP = grad(P)
+ * (complex64 [Nsp][NE][Nch]),
+ *   gradW[i*Nch + k] = sum_{s,e} Re(gradP[s][e][k] conj(in[s+i][e][k])).
+ * `iq` holds Nsp + Ntaps - 1 spectra of int8 I/Q.  Partial sums are doubles
+ * in `workspace` (at least Ntaps*Nch*8 bytes; up to 64 times that is used
+ * for more parallelism), reduced in a fixed order (deterministic). */
+MDT_API mdt_status mdt_pfb_tap_grad(int ne, int nch, int ntaps, int nsp, const void *gradP,
+                                    const int8_t *iq, float *gradW, void *workspace,
+                                    size_t workspace_bytes, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
  * One integration without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory
  * themselves -- a real-time ingest loop in which cudaMalloc's implicit device

@@ -26,5 +26,6 @@ from .binding import (  # noqa: F401
     fengine_x16, xengine_tc, x16_bytes, fengine_c64b, fx_integrate_static,
     FxPlan, FxBatch, MDT_PREC_FP32, MDT_PREC_FP16, MDT_PREC_BF16, MDT_PREC_INT8,
     fengine_q8, xengine_q8,
+    apply_gains, xengine_adjoint_f32, gain_adjoint, pfb_tap_grad,
 )
 from . import configs  # noqa: F401

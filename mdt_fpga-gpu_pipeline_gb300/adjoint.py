@@ -1,0 +1,153 @@
+"""Differentiation through the FX path: torch.autograd.Function over the
+library's forward and adjoint kernels, and per-antenna complex-gain
+calibration by gradient descent.
+
+Forward (FP32, the plan's arithmetic):
+    X = F-engine(iq; taps)      mdt_fengine_f32: PpS_Batch -> FFT -> reorder
+                                (reference MDT_device_functions.cu PpS_Batch,
+                                MDT_OneStation_client.cu:1083-1114)
+    Y = diag(gains) X           mdt_apply_gains, gains [Nch][NE] complex
+    V = Y Y^H / Nsp             mdt_xengine_f32 (replaces cublasCgemmBatched,
+                                MDT_OneStation_client.cu:1128)
+Backward (hand-written adjoints, no PyTorch math on the path):
+    dY     = (G + G^H) Y / Nsp          mdt_xengine_adjoint_f32
+    dgains = sum_s dY conj(X)           mdt_gain_adjoint
+    dF     = reorder^T(conj(g) dY)      mdt_gain_adjoint
+    dP     = DFT^H dF                   mdt_fft_c2c(direction=+1)
+    dtaps  = sum Re(dP conj(in))        mdt_pfb_tap_grad
+The F-engine output is recomputed in the backward pass instead of being kept
+from the forward pass (it is Nch*Nsp*NE*8 bytes, the largest tensor here).
+Gradients follow PyTorch's complex convention, grad = dL/dRe + i dL/dIm.
+"""
+import torch
+
+from . import binding as B
+
+
+def _cplx(n, device):
+    return torch.empty(n, dtype=torch.complex64, device=device)
+
+
+def _fengine(iq, taps, ne, nch, ntaps, nsp):
+    X = _cplx(nch * nsp * ne, iq.device)
+    B.fengine_f32(ne, nch, ntaps, nsp, iq, taps, X)
+    return X
+
+
+class FxCorrelate(torch.autograd.Function):
+    """V[c, q, r] = (1/Nsp) sum_s Y[c,s,r] conj(Y[c,s,q]),  Y = gains * F(iq; taps).
+
+    iq: int8 CUDA tensor of (Nsp + Ntaps - 1) * NE * Nch * 2 values (no gradient);
+    taps: float32 [Ntaps * Nch] (window, tap-major); gains: complex64 [Nch, NE].
+    Returns complex64 [Nch, NE, NE] (the column-major visibility layout)."""
+
+    @staticmethod
+    def forward(ctx, iq, taps, gains, ne, nch, ntaps, nsp):
+        if not (iq.is_cuda and taps.is_cuda and gains.is_cuda):
+            raise B.MdtError("FxCorrelate: inputs must be CUDA tensors")
+        taps = taps.detach().contiguous().to(torch.float32)
+        gains = gains.detach().contiguous().to(torch.complex64)
+        if taps.numel() != ntaps * nch or gains.numel() != nch * ne:
+            raise B.MdtError("FxCorrelate: taps must hold Ntaps*Nch and gains Nch*NE values")
+        X = _fengine(iq, taps, ne, nch, ntaps, nsp)
+        Y = torch.empty_like(X)
+        B.apply_gains(ne, nch, nsp, X, gains, Y)
+        del X
+        V = torch.empty(nch, ne, ne, dtype=torch.complex64, device=iq.device)
+        B.xengine_f32(ne, nch, nsp, Y, ne, nsp * ne, 1.0 / nsp, V)
+        ctx.save_for_backward(iq, taps, gains)
+        ctx.dims = (ne, nch, ntaps, nsp)
+        return V
+
+    @staticmethod
+    def backward(ctx, gV):
+        iq, taps, gains = ctx.saved_tensors
+        ne, nch, ntaps, nsp = ctx.dims
+        need_taps, need_gains = ctx.needs_input_grad[1], ctx.needs_input_grad[2]
+        if not (need_taps or need_gains):
+            return (None,) * 7
+        G = gV.detach().to(torch.complex64).contiguous()
+        X = _fengine(iq, taps, ne, nch, ntaps, nsp)  # recomputed, not stored
+        Y = torch.empty_like(X)
+        B.apply_gains(ne, nch, nsp, X, gains, Y)
+        dY = torch.empty_like(X)
+        B.xengine_adjoint_f32(ne, nch, nsp, G, Y, dY, 1.0 / nsp)
+        dgains = torch.empty(nch, ne, dtype=torch.complex64, device=iq.device) \
+            if need_gains else None
+        dF = Y if need_taps else None  # Y is dead from here on: reuse it
+        B.gain_adjoint(ne, nch, nsp, dY, X=X if need_gains else None, gains=gains,
+                       dgains=dgains, dF=dF)
+        dtaps = None
+        if need_taps:
+            del X
+            dP = dY  # dY is consumed: the inverse FFT writes over it
+            B.fft_c2c(dF, dP, nsp * ne, nch, B.CUFFT_INVERSE)
+            dtaps = torch.empty(ntaps * nch, dtype=torch.float32, device=iq.device)
+            ws = torch.empty(ntaps * nch * 64, dtype=torch.float64, device=iq.device)
+            B.pfb_tap_grad(ne, nch, ntaps, nsp, dP, iq, dtaps, ws)
+        return None, dtaps, dgains, None, None, None, None
+
+
+def _sqnorm(z):
+    # |z|^2 through real and imaginary parts: abs() has no gradient at 0
+    return (z.real ** 2 + z.imag ** 2).sum()
+
+
+def fx_correlate(iq, taps, gains, ne, nch, ntaps, nsp):
+    """Differentiable FX correlation (see FxCorrelate)."""
+    return FxCorrelate.apply(iq, taps, gains, ne, nch, ntaps, nsp)
+
+
+def baseline_mask(ne, device):
+    """True on the pairs a < b of the [q, r] visibility layout (r < q)."""
+    idx = torch.arange(ne, device=device)
+    return idx[None, :] < idx[:, None]
+
+
+def gain_error(est, true):
+    """Relative error of estimated gains after removing each channel's global
+    phase (which the baseline loss cannot see):  ||est e^{i phi} - true|| /
+    ||true||, phi per channel from the best alignment; float."""
+    est = est.to(torch.complex128)
+    true = true.to(torch.complex128)
+    ph = (est.conj() * true).sum(dim=1, keepdim=True)
+    ph = ph / ph.abs().clamp_min(1e-300)
+    return float(torch.linalg.vector_norm(est * ph - true) / torch.linalg.vector_norm(true))
+
+
+def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9, step=0.5,
+                true_gains=None, callback=None):
+    """Per-antenna, per-channel complex gains by gradient descent.
+
+    Loss  L(g) = sum_c sum_{a<b} |V(g)_ab - data_ab|^2  with V(g) the FX
+    correlation of `iq` under gains g (FxCorrelate; since V(g)_ab =
+    g_a conj(g_b) model_ab, this is the loss |data - g_a g_b^* model|^2 against
+    the source model `model` = V(1)).  Gradients come from the adjoint
+    kernels; each step is preconditioned per (channel, antenna) by the
+    diagonal of the Gauss-Newton normal equations,
+        h_ca = sum_{b != a} |g_cb|^2 |model_c,ab|^2,
+    computed with the iterate in FP64 on the GPU:  g <- g - step * grad / (2h).
+    Stops when the relative loss drops below `tol` (or after `iters` steps).
+    Returns (gains complex64 [Nch, NE], history list of (loss, error or None))."""
+    dev = iq.device
+    mask = baseline_mask(ne, dev)
+    m2 = model.detach().to(torch.complex128).abs() ** 2  # [c, q, r]
+    m2 = m2 * (1 - torch.eye(ne, dtype=torch.float64, device=dev))
+    g = torch.ones(nch, ne, dtype=torch.complex128, device=dev)
+    data = data.detach()
+    dnorm = float(_sqnorm(data[:, mask]))
+    hist = []
+    for _ in range(iters):
+        gv = g.to(torch.complex64).requires_grad_(True)
+        V = fx_correlate(iq, taps, gv, ne, nch, ntaps, nsp)
+        loss = _sqnorm((V - data)[:, mask])
+        loss.backward()
+        err = gain_error(g, true_gains) if true_gains is not None else None
+        hist.append((float(loss.detach()) / dnorm, err))
+        if callback is not None:
+            callback(len(hist), hist[-1])
+        if hist[-1][0] < tol:
+            break
+        h = torch.einsum("cb,cab->ca", g.abs() ** 2, m2)  # model is Hermitian
+        g = g - step * gv.grad.to(torch.complex128) / (2 * h)
+    return g.to(torch.complex64), hist

@@ -86,6 +86,10 @@ def _declare(L):
         "mdt_fx_batch_autotune": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
         "mdt_fx_batch_execute": ([_P, _P, _P, _I], _I),
         "mdt_fx_batch_check": ([_P], _I),
+        "mdt_apply_gains": ([_I, _I, _I, _P, _P, _P, _P], _I),
+        "mdt_xengine_adjoint_f32": ([_I, _I, _I, _P, _P, _P, _F, _P], _I),
+        "mdt_gain_adjoint": ([_I, _I, _I, _P, _P, _P, _P, _P, _P], _I),
+        "mdt_pfb_tap_grad": ([_I, _I, _I, _I, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
         "cufftPlan1d": ([ctypes.POINTER(_I), _I, _I, _I], _I),
         "cufftSetStream": ([_I, _P], _I),
         "cufftExecC2C": ([_I, _P, _P, _I], _I),
@@ -304,6 +308,28 @@ def fx_integrate_static(ne, nch, ntaps, nsp, iq, window, vis, stream=None):
     """One FP32 integration with no device allocation (mdt_fx_integrate_static)."""
     check(lib().mdt_fx_integrate_static(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(vis),
                                         stream_handle(stream)), "mdt_fx_integrate_static")
+
+
+# ----------------------------------------------------------- adjoints
+def apply_gains(ne, nch, nsp, X, gains, Y, stream=None):
+    check(lib().mdt_apply_gains(ne, nch, nsp, ptr(X), ptr(gains), ptr(Y), stream_handle(stream)),
+          "apply_gains")
+
+
+def xengine_adjoint_f32(ne, nch, nsp, G, Y, dY, scale, stream=None):
+    check(lib().mdt_xengine_adjoint_f32(ne, nch, nsp, ptr(G), ptr(Y), ptr(dY), scale,
+                                        stream_handle(stream)), "xengine_adjoint_f32")
+
+
+def gain_adjoint(ne, nch, nsp, dY, X=None, gains=None, dgains=None, dF=None, stream=None):
+    check(lib().mdt_gain_adjoint(ne, nch, nsp, ptr(dY), ptr(X), ptr(gains), ptr(dgains), ptr(dF),
+                                 stream_handle(stream)), "gain_adjoint")
+
+
+def pfb_tap_grad(ne, nch, ntaps, nsp, gradP, iq, gradW, workspace, stream=None):
+    nbytes = workspace.numel() * workspace.element_size()
+    check(lib().mdt_pfb_tap_grad(ne, nch, ntaps, nsp, ptr(gradP), ptr(iq), ptr(gradW),
+                                 ptr(workspace), nbytes, stream_handle(stream)), "pfb_tap_grad")
 
 
 # ----------------------------------------------------------- plan API
