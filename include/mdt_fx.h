@@ -322,6 +322,94 @@ MDT_API mdt_status mdt_fx_batch_execute(mdt_fx_batch batch, const int8_t *const 
 MDT_API mdt_status mdt_fx_batch_check(mdt_fx_batch batch);
 
 /* ------------------------------------------------------------------------
+ * GPU depacketiser.  Replaces the host loop of the reference client's rank 1
+ * (MDT_OneStation_client.cu:846-907), which unpacks each SNAP UDP packet into
+ * the [spectrum][element][channel] input stack.
+ *
+ * A packet: `words_header` uint32 header words ([0] station, [1] SNAP board,
+ * [2] packet counter; the reference has 4), then for each of `sper_element`
+ * samples i, for each input j < inputs_per_snap[snap]: the sample of input j
+ * -- two uint32 (re, im; int32 fixed point with 19 fraction bits) when
+ * sample_bits = 32 (the reference's format), or two int8 (re, im) when
+ * sample_bits = 8.  Packets sit `packet_bytes` apart in the batch buffer.
+ * Sample i of a packet is element-sample counter*sper_element + i, i.e.
+ * spectrum (that / Nch), channel (that % Nch); its element is
+ * station*inputs_per_station + sum_{k<snap} inputs_per_snap[k] + j.
+ * The reference's SNAP layout: inputs_per_station 38, 4 SNAPs of
+ * {10, 10, 10, 8} inputs (MDT_OneStation_client.h:64-68). */
+#define MDT_MAX_SNAPS 8
+typedef struct {
+    int words_header;         /* >= 3 */
+    int sper_element;         /* samples per element per packet */
+    int inputs_per_station;
+    int nsnap;                /* <= MDT_MAX_SNAPS */
+    int inputs_per_snap[MDT_MAX_SNAPS];
+    int sample_bits;          /* 32: int32 x 2^-19 -> complex64; 8: int8 I/Q -> int8 I/Q */
+    int packet_bytes;         /* stride between packets, multiple of 4 */
+} mdt_packet_format;
+
+/* Device-side counters (zero them before the first call; they accumulate). */
+typedef struct {
+    unsigned long long accepted;   /* packets written into the window */
+    unsigned long long outside;    /* packets whose counter lies outside the window */
+    unsigned long long bad;        /* bad station / SNAP, or elements past NE */
+    unsigned long long duplicate;  /* further arrivals of a slot already seen */
+    unsigned long long missing;    /* slots zero-filled by mdt_depacketise_finish */
+} mdt_depack_stats;
+
+/* Number of uint32 arrival counters `seen` needs for a window:
+ * ceil(NE / inputs_per_station) * nsnap * (packet slots touching the window). */
+MDT_API mdt_status mdt_depacketise_seen_words(const mdt_packet_format *fmt, int ne, int nch,
+                                              long long sample0, int nspectra, size_t *words);
+
+/* Writes the samples of `npackets` packets (device buffer) that fall in the
+ * window of element-samples [sample0, sample0 + nspectra*Nch) (sample0 a
+ * multiple of Nch) into `out`: complex64 [nspectra][NE][Nch] for 32-bit
+ * samples (bit-identical to the reference's conversion, which maps
+ * 0x80000000 to +4096.0), int8 [nspectra][NE][Nch][2] for 8-bit samples.
+ * `seen` (zeroed once) counts arrivals per (station, SNAP, slot).  Can be
+ * called many times per window as packets arrive; duplicate packets write the
+ * same place (the value of one of them remains). */
+MDT_API mdt_status mdt_depacketise(const mdt_packet_format *fmt, const void *packets, int npackets,
+                                   int ne, int nch, long long sample0, int nspectra, void *out,
+                                   unsigned int *seen, mdt_depack_stats *stats,
+                                   cudaStream_t stream);
+
+/* Closes a window: zero-fills the samples of every packet slot that never
+ * arrived (gap detection; stats->missing counts them) and clears `seen`. */
+MDT_API mdt_status mdt_depacketise_finish(const mdt_packet_format *fmt, int ne, int nch,
+                                          long long sample0, int nspectra, void *out,
+                                          unsigned int *seen, mdt_depack_stats *stats,
+                                          cudaStream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Output formatter and writers.  The reference writes each integration as
+ * CSV lines "j,p,k,q,z,re,im" ("%ld,%d,%ld,%d,%ld,%.6f,%.6f") for
+ * j < Nelements, p < Npols, k >= j, q >= p, channel z = 0..Nch-1 fftshifted
+ * (z <- channel (z + Nch/2) % Nch), value V[i][(k*Npols+q)*NE + (j*Npols+p)]
+ * (MDT_OneStation_client.cu:1239-1266).
+ *
+ * Number of baselines in that order: Npols(Npols+1)/2 * Nelements(Nelements+1)/2. */
+MDT_API mdt_status mdt_num_baselines(int nelements, int npols, long *nbl);
+
+/* GPU gather of the visibilities (complex64 [Nch][NE][NE] column-major, NE =
+ * Nelements*Npols, device) into out[bl][z] (complex64, device), baselines in
+ * the reference's order, channels fftshifted when `fftshift` (Nch even). */
+MDT_API mdt_status mdt_format_baselines(int nelements, int npols, int nch, const void *vis,
+                                        void *out, int fftshift, cudaStream_t stream);
+
+/* Host writers of a formatted buffer (host memory, complex64 [nbl][Nch]).
+ * CSV: byte-identical to the reference's fprintf lines, formatted by
+ * `nthreads` threads (<= 0: all cores) and written in order; `append` adds
+ * to an existing file.  Binary: header {"MDTVIS01", int32 Nelements, Npols,
+ * Nch, nbl, 8 reserved bytes}, int32 [nbl][4] (j, p, k, q), complex64
+ * [nbl][Nch].  Neither needs a GPU. */
+MDT_API mdt_status mdt_write_csv(const char *path, int nelements, int npols, int nch,
+                                 const void *formatted, int append, int nthreads);
+MDT_API mdt_status mdt_write_binary(const char *path, int nelements, int npols, int nch,
+                                    const void *formatted, int append);
+
+/* ------------------------------------------------------------------------
  * Adjoints (differentiation through the FX path).  No counterpart in the
  * reference, which only runs forward; these are the backward halves of
  * mdt_fengine_f32 -> gains -> mdt_xengine_f32 for gain calibration and PFB

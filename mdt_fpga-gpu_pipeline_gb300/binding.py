@@ -86,6 +86,14 @@ def _declare(L):
         "mdt_fx_batch_autotune": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
         "mdt_fx_batch_execute": ([_P, _P, _P, _I], _I),
         "mdt_fx_batch_check": ([_P], _I),
+        "mdt_depacketise_seen_words": ([_P, _I, _I, ctypes.c_longlong, _I,
+                                        ctypes.POINTER(ctypes.c_size_t)], _I),
+        "mdt_depacketise": ([_P, _P, _I, _I, _I, ctypes.c_longlong, _I, _P, _P, _P, _P], _I),
+        "mdt_depacketise_finish": ([_P, _I, _I, ctypes.c_longlong, _I, _P, _P, _P, _P], _I),
+        "mdt_num_baselines": ([_I, _I, ctypes.POINTER(_L)], _I),
+        "mdt_format_baselines": ([_I, _I, _I, _P, _P, _I, _P], _I),
+        "mdt_write_csv": ([ctypes.c_char_p, _I, _I, _I, _P, _I, _I], _I),
+        "mdt_write_binary": ([ctypes.c_char_p, _I, _I, _I, _P, _I], _I),
         "mdt_apply_gains": ([_I, _I, _I, _P, _P, _P, _P], _I),
         "mdt_xengine_adjoint_f32": ([_I, _I, _I, _P, _P, _P, _F, _P], _I),
         "mdt_gain_adjoint": ([_I, _I, _I, _P, _P, _P, _P, _P, _P], _I),
@@ -308,6 +316,84 @@ def fx_integrate_static(ne, nch, ntaps, nsp, iq, window, vis, stream=None):
     """One FP32 integration with no device allocation (mdt_fx_integrate_static)."""
     check(lib().mdt_fx_integrate_static(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(vis),
                                         stream_handle(stream)), "mdt_fx_integrate_static")
+
+
+# ----------------------------------------------------------- depacketiser
+MDT_MAX_SNAPS = 8
+STATS_FIELDS = ("accepted", "outside", "bad", "duplicate", "missing")
+
+
+class PacketFormat(ctypes.Structure):
+    """mdt_packet_format (include/mdt_fx.h)."""
+    _fields_ = [("words_header", _I), ("sper_element", _I), ("inputs_per_station", _I),
+                ("nsnap", _I), ("inputs_per_snap", _I * MDT_MAX_SNAPS), ("sample_bits", _I),
+                ("packet_bytes", _I)]
+
+
+def packet_format(sper_element, inputs_per_snap=(10, 10, 10, 8), inputs_per_station=38,
+                  words_header=4, sample_bits=32, packet_bytes=None):
+    """A packet format; the defaults are the reference's SNAP layout
+    (MDT_OneStation_client.h:64-68) and its packet size, which fits the
+    largest SNAP ((2 + 10*SperElement)*2 words, MDT_OneStation_client.cu:353)."""
+    f = PacketFormat()
+    f.words_header = words_header
+    f.sper_element = sper_element
+    f.inputs_per_station = inputs_per_station
+    f.nsnap = len(inputs_per_snap)
+    for k, n in enumerate(inputs_per_snap):
+        f.inputs_per_snap[k] = n
+    f.sample_bits = sample_bits
+    if packet_bytes is None:
+        per = 8 if sample_bits == 32 else 2
+        packet_bytes = 4 * words_header + sper_element * max(inputs_per_snap) * per
+        packet_bytes = (packet_bytes + 3) // 4 * 4
+    f.packet_bytes = packet_bytes
+    return f
+
+
+def depacketise_seen_words(fmt, ne, nch, sample0, nspectra):
+    n = ctypes.c_size_t()
+    check(lib().mdt_depacketise_seen_words(ctypes.byref(fmt), ne, nch, sample0, nspectra,
+                                           ctypes.byref(n)), "depacketise_seen_words")
+    return n.value
+
+
+def depacketise(fmt, packets, npackets, ne, nch, sample0, nspectra, out, seen, stats,
+                stream=None):
+    """stats: device int64 tensor of 5 counters (STATS_FIELDS)."""
+    check(lib().mdt_depacketise(ctypes.byref(fmt), ptr(packets), npackets, ne, nch, sample0,
+                                nspectra, ptr(out), ptr(seen), ptr(stats),
+                                stream_handle(stream)), "depacketise")
+
+
+def depacketise_finish(fmt, ne, nch, sample0, nspectra, out, seen, stats, stream=None):
+    check(lib().mdt_depacketise_finish(ctypes.byref(fmt), ne, nch, sample0, nspectra, ptr(out),
+                                       ptr(seen), ptr(stats), stream_handle(stream)),
+          "depacketise_finish")
+
+
+# ----------------------------------------------------------- output
+def num_baselines(nelements, npols=1):
+    n = _L()
+    check(lib().mdt_num_baselines(nelements, npols, ctypes.byref(n)), "num_baselines")
+    return n.value
+
+
+def format_baselines(nelements, npols, nch, vis, out, fftshift=True, stream=None):
+    check(lib().mdt_format_baselines(nelements, npols, nch, ptr(vis), ptr(out),
+                                     1 if fftshift else 0, stream_handle(stream)),
+          "format_baselines")
+
+
+def write_csv(path, nelements, npols, nch, formatted, append=False, nthreads=0):
+    """formatted: host buffer (numpy complex64 [nbl][Nch] or a CPU tensor)."""
+    check(lib().mdt_write_csv(os.fsencode(path), nelements, npols, nch, _host_ptr(formatted),
+                              1 if append else 0, nthreads), "write_csv")
+
+
+def write_binary(path, nelements, npols, nch, formatted, append=False):
+    check(lib().mdt_write_binary(os.fsencode(path), nelements, npols, nch,
+                                 _host_ptr(formatted), 1 if append else 0), "write_binary")
 
 
 # ----------------------------------------------------------- adjoints

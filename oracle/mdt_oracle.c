@@ -198,3 +198,75 @@ void mdt_oracle_synth_iq(uint64_t seed, int ne, int nch, long s0, long nsp,
         }
     }
 }
+
+/* ------------------------------------------------------------------------
+ * Depacketiser, restating the reference client's rank-1 loop
+ * (MDT_OneStation_client.cu:846-907) over a window of element-samples
+ * [sample0, sample0 + nspectra*nch) instead of its two Nspectra stacks.
+ * Packets are processed in order; samples outside the window are skipped.
+ * sample_bits 32: two uint32 words per sample, the reference's conversion
+ * (MDT_OneStation_client.cu:896-907): w >= 2^31 -> -(2^-19) * (int)(2^32 - w)
+ * in double (2^32 - w wraps to INT_MIN through the int for w = 2^31, giving
+ * +4096), else (2^-19) * (int)w; rounded to float.  sample_bits 8: int8 pairs
+ * copied.  stats[0..2] += accepted, outside, bad.  Returns 0. */
+static float mdt_fixed19(uint32_t w)
+{
+    const double lsb = 1.0 / 524288.0; /* 2^-19 */
+    double d;
+    if (w >= 0x80000000u) {
+        int32_t m = (int32_t)(uint32_t)(0x100000000ULL - (uint64_t)w); /* wraps at w = 2^31 */
+        d = -lsb * (double)m;
+    } else {
+        d = lsb * (double)(int32_t)w;
+    }
+    return (float)d;
+}
+
+int mdt_oracle_depacketise(int words_header, int sper, int ips, int nsnap,
+                           const int *inputs_per_snap, int sample_bits, long packet_bytes,
+                           const unsigned char *pkts, int npkt, int ne, int nch,
+                           long long sample0, int nspectra, void *out, long long *stats)
+{
+    const int nstation = (ne + ips - 1) / ips;
+    const long long wlen = (long long)nspectra * nch;
+    for (int p = 0; p < npkt; p++) {
+        const unsigned char *pk = pkts + (long)p * packet_bytes;
+        uint32_t hdr[3];
+        memcpy(hdr, pk, sizeof hdr);
+        if (hdr[1] >= (uint32_t)nsnap || hdr[0] >= (uint32_t)nstation) {
+            stats[2]++;
+            continue;
+        }
+        long elem0 = (long)hdr[0] * ips;
+        for (uint32_t k = 0; k < hdr[1]; k++) elem0 += inputs_per_snap[k];
+        const int nin = inputs_per_snap[hdr[1]];
+        if (elem0 + nin > ne) {
+            stats[2]++;
+            continue;
+        }
+        const long long first = (long long)hdr[2] * sper;
+        if (first + sper <= sample0 || first >= sample0 + wlen) {
+            stats[1]++;
+            continue;
+        }
+        stats[0]++;
+        for (int i = 0; i < sper; i++) {
+            const long long s = first + i - sample0;
+            if (s < 0 || s >= wlen) continue;
+            const long long spec = s / nch, chan = s % nch;
+            for (int j = 0; j < nin; j++) {
+                const long o = ((long)spec * ne + elem0 + j) * nch + chan;
+                const long b = 4L * words_header;
+                if (sample_bits == 32) {
+                    uint32_t w[2];
+                    memcpy(w, pk + b + 8L * ((long)i * nin + j), sizeof w);
+                    ((float *)out)[2 * o] = mdt_fixed19(w[0]);
+                    ((float *)out)[2 * o + 1] = mdt_fixed19(w[1]);
+                } else {
+                    memcpy((int8_t *)out + 2 * o, pk + b + 2L * ((long)i * nin + j), 2);
+                }
+            }
+        }
+    }
+    return 0;
+}

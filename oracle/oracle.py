@@ -55,6 +55,8 @@ def lib():
             getattr(L, "mdt_oracle_fft_rows" + suf).restype = i
             getattr(L, "mdt_oracle_fx" + suf).argtypes = [i, i, i, i, P, P, i, P, P]
             getattr(L, "mdt_oracle_fx" + suf).restype = i
+        L.mdt_oracle_depacketise.argtypes = [i, i, i, i, P, i, l, P, i, i, i,
+                                             ctypes.c_longlong, i, P, P]
         L.mdt_oracle_xengine_f64.argtypes = [i, i, i, P, d, P]
         L.mdt_oracle_xengine_f32.argtypes = [i, i, i, P, ctypes.c_float, P]
         _lib = L
@@ -168,3 +170,24 @@ def synth_iq(seed, ne, nch, s0, nsp, sigma_q8, tone_q16=None, src_sigma_q8=None,
                               None if ss is None else _p(ss),
                               None if sd is None else _p(sd), _p(out))
     return out
+
+
+def depacketise(fmt, pkts, npkt, ne, nch, sample0, nspectra, out=None):
+    """Restated rank-1 depacketise loop (MDT_OneStation_client.cu:846-907)
+    into a window; fmt is a dict with words_header, sper_element,
+    inputs_per_station, inputs_per_snap (list), sample_bits, packet_bytes.
+    Returns (out, [accepted, outside, bad]); out is complex64
+    [nspectra][ne][nch] (32-bit samples) or int8 [nspectra][ne][nch][2],
+    zero where no packet wrote (unless `out` is given)."""
+    bits = fmt["sample_bits"]
+    if out is None:
+        out = (np.zeros((nspectra, ne, nch), np.complex64) if bits == 32
+               else np.zeros((nspectra, ne, nch, 2), np.int8))
+    ips = np.ascontiguousarray(fmt["inputs_per_snap"], np.int32)
+    pk = np.ascontiguousarray(pkts).view(np.uint8)
+    stats = np.zeros(3, np.int64)
+    lib().mdt_oracle_depacketise(fmt["words_header"], fmt["sper_element"],
+                                 fmt["inputs_per_station"], len(ips), _p(ips), bits,
+                                 fmt["packet_bytes"], _p(pk), npkt, ne, nch, sample0, nspectra,
+                                 _p(out), _p(stats))
+    return out, stats.tolist()
