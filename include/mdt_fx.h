@@ -383,6 +383,40 @@ MDT_API mdt_status mdt_depacketise_finish(const mdt_packet_format *fmt, int ne, 
                                           cudaStream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Streaming ingest pipeline: host packets -> pinned staging ring -> GPU
+ * depacketiser -> fused F/X plan (PFB history carried) -> optional output
+ * formatter -> pinned output ring.  Replaces the reference client's rank 1-3
+ * chain and its MPI handshakes (MDT_OneStation_client.cu:846-1234) on one GPU.
+ *
+ * Integration n covers element-samples [S(n), S(n) + len(n)): window 0 is
+ * Nsp + Ntaps - 1 spectra from sample 0, window n >= 1 the Nsp spectra after
+ * (Ntaps - 1 + n*Nsp)*Nch.  Two windows are open at a time; a packet for a
+ * later window closes the oldest (missing packets zero-filled and counted),
+ * packets for closed windows are dropped as late.  Packets must be 8-bit
+ * (int8 I/Q) in the given format, at most `max_packets` per push; they are
+ * copied, so the caller's buffer is free when push returns.  Results come
+ * back in order: complex64 [Nch][NE][NE] (formatted = 0) or the
+ * baseline-major fftshifted form of mdt_format_baselines (formatted = 1,
+ * Npols = 1).  At most 3 results wait for mdt_ingest_pop; a push that would
+ * close more returns MDT_ERR_STATE and consumes nothing.  From the third
+ * integration on, each integration's F/X work is one CUDA graph launch. */
+typedef struct mdt_ingest_s *mdt_ingest;
+MDT_API mdt_status mdt_ingest_create(const mdt_fx_desc *desc, const mdt_packet_format *fmt,
+                                     int max_packets, int formatted, mdt_ingest *ingest);
+MDT_API mdt_status mdt_ingest_destroy(mdt_ingest ingest);
+MDT_API mdt_status mdt_ingest_set_window(mdt_ingest ingest, const float *window);
+MDT_API mdt_status mdt_ingest_push(mdt_ingest ingest, const void *packets, int npackets);
+/* Closes the open windows that hold any packet (end of stream). */
+MDT_API mdt_status mdt_ingest_flush(mdt_ingest ingest);
+/* Oldest finished integration: its index (-1 if none is ready -- or none is
+ * pending -- when wait = 0, or none is pending when wait != 0), its result
+ * copied to `out` (host, out_bytes; may be NULL) and its window's counters. */
+MDT_API mdt_status mdt_ingest_pop(mdt_ingest ingest, void *out, long long *integration,
+                                  mdt_depack_stats *stats, int wait);
+MDT_API mdt_status mdt_ingest_counters(mdt_ingest ingest, long long *late, long long *bad,
+                                       long long *next_window, size_t *out_bytes);
+
+/* ------------------------------------------------------------------------
  * Output formatter and writers.  The reference writes each integration as
  * CSV lines "j,p,k,q,z,re,im" ("%ld,%d,%ld,%d,%ld,%.6f,%.6f") for
  * j < Nelements, p < Npols, k >= j, q >= p, channel z = 0..Nch-1 fftshifted

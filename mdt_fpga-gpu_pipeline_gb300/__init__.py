@@ -28,6 +28,6 @@ from .binding import (  # noqa: F401
     fengine_q8, xengine_q8,
     apply_gains, xengine_adjoint_f32, gain_adjoint, pfb_tap_grad,
     PacketFormat, packet_format, depacketise_seen_words, depacketise, depacketise_finish,
-    STATS_FIELDS, num_baselines, format_baselines, write_csv, write_binary,
+    STATS_FIELDS, Ingest, num_baselines, format_baselines, write_csv, write_binary,
 )
 from . import configs  # noqa: F401

@@ -94,6 +94,16 @@ def _declare(L):
         "mdt_format_baselines": ([_I, _I, _I, _P, _P, _I, _P], _I),
         "mdt_write_csv": ([ctypes.c_char_p, _I, _I, _I, _P, _I, _I], _I),
         "mdt_write_binary": ([ctypes.c_char_p, _I, _I, _I, _P, _I], _I),
+        "mdt_ingest_create": ([_P, _P, _I, _I, ctypes.POINTER(_P)], _I),
+        "mdt_ingest_destroy": ([_P], _I),
+        "mdt_ingest_set_window": ([_P, _P], _I),
+        "mdt_ingest_push": ([_P, _P, _I], _I),
+        "mdt_ingest_flush": ([_P], _I),
+        "mdt_ingest_pop": ([_P, _P, ctypes.POINTER(ctypes.c_longlong), _P, _I], _I),
+        "mdt_ingest_counters": ([_P, ctypes.POINTER(ctypes.c_longlong),
+                                 ctypes.POINTER(ctypes.c_longlong),
+                                 ctypes.POINTER(ctypes.c_longlong),
+                                 ctypes.POINTER(ctypes.c_size_t)], _I),
         "mdt_apply_gains": ([_I, _I, _I, _P, _P, _P, _P], _I),
         "mdt_xengine_adjoint_f32": ([_I, _I, _I, _P, _P, _P, _F, _P], _I),
         "mdt_gain_adjoint": ([_I, _I, _I, _P, _P, _P, _P, _P, _P], _I),
@@ -370,6 +380,65 @@ def depacketise_finish(fmt, ne, nch, sample0, nspectra, out, seen, stats, stream
     check(lib().mdt_depacketise_finish(ctypes.byref(fmt), ne, nch, sample0, nspectra, ptr(out),
                                        ptr(seen), ptr(stats), stream_handle(stream)),
           "depacketise_finish")
+
+
+class _DepackStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_ulonglong) for n in STATS_FIELDS]
+
+
+class Ingest:
+    """Streaming ingest pipeline (mdt_ingest_*): host int8 packets in,
+    integrations out, in order."""
+
+    def __init__(self, nelements, nchannels, ntaps, nspectra, fmt, max_packets,
+                 formatted=False, precision=MDT_PREC_FP32):
+        self._h = None
+        d = _Desc(nelements, nchannels, ntaps, nspectra, precision)
+        self.fmt = fmt
+        h = _P()
+        check(lib().mdt_ingest_create(ctypes.byref(d), ctypes.byref(fmt), max_packets,
+                                      1 if formatted else 0, ctypes.byref(h)), "ingest_create")
+        self._h = h
+        self.out_bytes = self.counters()["out_bytes"]
+
+    def set_window(self, window):
+        check(lib().mdt_ingest_set_window(self._h, ptr(window)), "ingest_set_window")
+
+    def push(self, packets, npackets=None):
+        """packets: host numpy uint8 [n][packet_bytes] (or a raw address)."""
+        n = len(packets) if npackets is None else npackets
+        check(lib().mdt_ingest_push(self._h, _host_ptr(packets), n), "ingest_push")
+
+    def flush(self):
+        check(lib().mdt_ingest_flush(self._h), "ingest_flush")
+
+    def pop(self, out=None, wait=True):
+        """Returns (integration index or -1, stats dict); fills `out` (host
+        buffer of out_bytes) when given."""
+        it = ctypes.c_longlong()
+        st = _DepackStats()
+        check(lib().mdt_ingest_pop(self._h, None if out is None else _host_ptr(out),
+                                   ctypes.byref(it), ctypes.byref(st), 1 if wait else 0),
+              "ingest_pop")
+        return it.value, {n: getattr(st, n) for n in STATS_FIELDS}
+
+    def counters(self):
+        late, bad, nxt = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        ob = ctypes.c_size_t()
+        check(lib().mdt_ingest_counters(self._h, ctypes.byref(late), ctypes.byref(bad),
+                                        ctypes.byref(nxt), ctypes.byref(ob)), "ingest_counters")
+        return dict(late=late.value, bad=bad.value, next_window=nxt.value, out_bytes=ob.value)
+
+    def close(self):
+        if self._h:
+            check(lib().mdt_ingest_destroy(self._h), "ingest_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ----------------------------------------------------------- output
