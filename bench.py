@@ -19,9 +19,10 @@ than L2, so no L2 flush is needed between steps.
 cores.  The reference has no CPU FX code, so this is the oracle port (FP32,
 OpenMP, all host threads) on a bounded sample of the same workload.
 
-Multi-GPU (torchrun): replicas only -- every rank runs its own 16-integration
-stream (different seed), no data-path collective; value = all ranks'
-samples / max rank time ("scaling": "weak").
+Multi-GPU (torchrun): replicas only -- rank r runs integrations
+[16r, 16r + 16) of one stream (its own span of the counter-based generator,
+lead-in included), no data-path collective; value = all ranks' samples / max
+rank time ("scaling": "weak").
 """
 import argparse
 import importlib
@@ -326,9 +327,15 @@ def run_ours(args, cfg):
     def t(a):
         return None if a is None else torch.from_numpy(np.ascontiguousarray(a)).to(dev)
 
+    # replicas only: rank r takes integrations [r*nint, (r+1)*nint) of one
+    # stream and generates just its span (the generator is counter-based)
+    replicas = importlib.import_module("mdt_fpga-gpu_pipeline_gb300.replicas")
+    first_int, _ = replicas.integration_split(nint * world, rank, world)
+    s0, span = replicas.input_span(first_int, nint, nsp, ntaps)
+    assert span == total_sp
     iq = torch.empty(total_sp * sb, dtype=torch.int8, device=dev)
     ssig, sdel = cfg.sources()
-    mdt.synth_iq(cfg.seed + 7919 * rank, ne, nch, 0, total_sp, t(cfg.sigma_q8()), iq,
+    mdt.synth_iq(cfg.seed, ne, nch, s0, total_sp, t(cfg.sigma_q8()), iq,
                  tone_q16=t(cfg.tone_q16()), src_sigma_q8=t(ssig), src_delay=t(sdel))
     win = torch.empty(nch * ntaps, dtype=torch.float32, device=dev)
     mdt.window_hamming_sinc(nch, ntaps, win)
