@@ -153,7 +153,7 @@ MDT_API mdt_status mdt_fengine_c64b(int ne, int nch, int ntaps, int nsp, const i
 /* Fused F-engine for the tensor-core path: int8 I/Q -> PFB -> FFT -> output
  * scaled by `scale` (a power of two keeps it exact) and rounded to f16
  * (ab_fmt 0) or bf16 (ab_fmt 1) in the X16 operand layout:
- *   X16[c][kc][e][128 bytes], kc = 32-spectrum chunk (ceil(Nsp/32) chunks),
+ *   X16[kc][c][e][128 bytes], kc = 32-spectrum chunk (ceil(Nsp/32) chunks),
  *   e < NEp = NE rounded up to 16, row = [re(32 spectra) | im(32 spectra)],
  *   16-byte chunk j of row e stored at chunk j ^ (e & 7) (the K-major
  *   128-byte-swizzled layout the tensor cores read), spectra past Nsp zero.
@@ -162,6 +162,18 @@ MDT_API mdt_status mdt_fengine_c64b(int ne, int nch, int ntaps, int nsp, const i
 MDT_API mdt_status mdt_fengine_x16(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
                                    const float *window, void *X16, int ab_fmt, float scale,
                                    cudaStream_t stream);
+
+/* Tensor-core F-engine (Nch = 1024, Ntaps 4 or 8): same inputs and X16
+ * output layout as mdt_fengine_x16, with the 1024-point DFT done as two
+ * 32-point DFT matrix products on tcgen05 (f16 operands, FP32 accumulation,
+ * FP32 twiddles between them); the PFB output and the twiddled intermediate
+ * are rounded to f16 once each.  `err` (device int, zeroed by the caller) is
+ * set if a device wait timed out.  Replaces PpS_Batch -> cufftExecC2C ->
+ * ReorderFOutput (reference MDT_OneStation_client.cu:1083-1114) for the
+ * tensor-core X-engine. */
+MDT_API mdt_status mdt_fengine_tc(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                  const float *window, void *X16, int ab_fmt, float scale,
+                                  int *err, cudaStream_t stream);
 
 /* Exact-int8 F-engine: as mdt_fengine_x16 but the values are integers
  * clamp(rint(x * qscales[c]), -127, 127) (stored as f16, exactly). */

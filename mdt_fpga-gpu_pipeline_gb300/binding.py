@@ -71,6 +71,7 @@ def _declare(L):
         "mdt_fx_set_accumulator": ([_P, _P], _I),
         "mdt_fx_set_channel_scales": ([_P, _P], _I),
         "mdt_fx_get_channel_scales": ([_P, _P], _I),
+        "mdt_fengine_tc": ([_I, _I, _I, _I, _P, _P, _P, _I, _F, _P, _P], _I),
         "mdt_fengine_q8": ([_I, _I, _I, _I, _P, _P, _P, _P, _P], _I),
         "mdt_xengine_q8": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P], _I),
         "mdt_fx_integrate_static": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
@@ -296,6 +297,12 @@ def xengine_tc(ne, nch, nsp, X16, vis, vis_acc=None, err=None, ab_fmt=0, scale=1
                stream=None):
     check(lib().mdt_xengine_tc(ne, nch, nsp, ptr(X16), ab_fmt, scale, ptr(vis), ptr(vis_acc),
                                ptr(err), stream_handle(stream)), "xengine_tc")
+
+
+def fengine_tc(ne, nch, ntaps, nsp, iq, window, X16, err, ab_fmt=0, scale=1.0, stream=None):
+    """Tensor-core F-engine (Nch 1024): same output layout as fengine_x16."""
+    check(lib().mdt_fengine_tc(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X16), ab_fmt, scale,
+                               ptr(err), stream_handle(stream)), "fengine_tc")
 
 
 def fengine_q8(ne, nch, ntaps, nsp, iq, window, X16, qscales, stream=None):

@@ -27,7 +27,9 @@ namespace {
 struct Group {
     int nch, ntaps;
     int first, count;  // FJob entries [first, first + count)
-    long nblocks;
+    long nblocks;      // blocks of the SIMT F-engine launch
+    long nwork;        // work items of the tensor-core F-engine launch
+    bool tc;           // tensor-core F-engine (Nch 1024, Ntaps 4 or 8)
 };
 
 struct TuneChoice {
@@ -254,8 +256,10 @@ mdt_status autotune(mdt_fx_batch b)
 mdt_status launch_all(mdt_fx_batch b)
 {
     for (const Group &g : b->groups) {
-        mdt_status st = mdt::fengine_x16_batched(g.nch, g.ntaps, b->d_fjobs + g.first, g.count,
-                                                 g.nblocks, b->stream);
+        mdt_status st = g.tc ? mdt::fengine_tc_batched(g.ntaps, b->d_fjobs + g.first, g.count,
+                                                       g.nwork, b->d_err, b->stream)
+                             : mdt::fengine_x16_batched(g.nch, g.ntaps, b->d_fjobs + g.first,
+                                                        g.count, g.nblocks, b->stream);
         if (st != MDT_SUCCESS) return st;
     }
     return mdt::xengine_tc_batched(b->d_xjobs, b->d_work, b->nwork, b->d_err, b->stream);
@@ -324,7 +328,10 @@ MDT_API mdt_status mdt_fx_batch_create(const mdt_fx_desc *descs, int njobs, mdt_
         release(b);
         return st;
     }
-    // F-engine groups by (Nch, Ntaps), job tables
+    // F-engine groups by (Nch, Ntaps), job tables; MDT_FENGINE=simt keeps
+    // every group on the SIMT FFT F-engine
+    const char *fe = getenv("MDT_FENGINE");
+    const bool use_tc = !(fe && std::string(fe) == "simt");
     std::vector<int> order(njobs);
     for (int j = 0; j < njobs; j++) order[j] = j;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
@@ -336,7 +343,8 @@ MDT_API mdt_status mdt_fx_batch_create(const mdt_fx_desc *descs, int njobs, mdt_
         const mdt_fx_desc &d = b->d[j];
         if (b->groups.empty() || b->groups.back().nch != d.nchannels ||
             b->groups.back().ntaps != d.ntaps)
-            b->groups.push_back({d.nchannels, d.ntaps, idx, 0, 0});
+            b->groups.push_back({d.nchannels, d.ntaps, idx, 0, 0, 0,
+                                 use_tc && mdt::fengine_tc_shape(d.nchannels, d.ntaps)});
         Group &g = b->groups.back();
         mdt::FJob f;
         f.iq = nullptr;
@@ -348,7 +356,9 @@ MDT_API mdt_status mdt_fx_batch_create(const mdt_fx_desc *descs, int njobs, mdt_
         f.nkc = b->nkc[j];
         f.scale = b->scale[j];
         f.blk0 = (int)g.nblocks;
+        f.wk0 = (int)g.nwork;
         g.nblocks += mdt::fjob_blocks(d.nelements, b->nkc[j]);
+        g.nwork += mdt::fjob_tc_items(d.nelements, d.nspectra);
         g.count++;
         b->h_fjobs.push_back(f);
         b->fjob_of.push_back(j);
@@ -357,8 +367,8 @@ MDT_API mdt_status mdt_fx_batch_create(const mdt_fx_desc *descs, int njobs, mdt_
         const mdt_fx_desc &d = b->d[j];
         mdt::XJob x;
         x.X = b->x16 + b->x16_off[j];
-        x.chunk_bytes = (long)b->nep[j] * 128;
-        x.chan_bytes = (long)b->nkc[j] * x.chunk_bytes;
+        x.chan_bytes = (long)b->nep[j] * 128;
+        x.chunk_bytes = (long)d.nchannels * x.chan_bytes;
         x.ne = d.nelements;
         x.nep = b->nep[j];
         x.nkc = b->nkc[j];

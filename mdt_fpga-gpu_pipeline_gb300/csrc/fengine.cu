@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
 }
 
 // f16 / bf16 output (power-of-two scaled) in the tensor-core operand layout
-// of xengine_tc.cu:  X16[c][kc][e][128 B], row = [re(32 spectra) | im(32
+// of xengine_tc.cu:  X16[kc][c][e][128 B], row = [re(32 spectra) | im(32
 // spectra)], 16-byte chunk j stored at j ^ (e & 7).  The block's 8 spectra
 // are one 16-byte chunk of re and one of im per channel, written straight
 // from the transform's shared memory.
@@ -352,8 +352,9 @@ __global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
     const Block8 b(a.ne);
     fengine_block8<N, NT>(a, b, fsm);
 
-    uint8_t *rowbase = X16 + ((size_t)b.kc * nep + b.e) * 128;
-    const size_t cstride = (size_t)nkc * nep * 128;
+    // X16[kc][c][e][128 B]: rows of one (chunk, channel) are contiguous
+    uint8_t *rowbase = X16 + ((size_t)b.kc * N * nep + b.e) * 128;
+    const size_t cstride = (size_t)nep * 128;
     const int pre = (b.jsub ^ (b.e & 7)) << 4, pim = ((4 + b.jsub) ^ (b.e & 7)) << 4;
     for (int c = threadIdx.x; c < N; c += C::THREADS) {
         float2 v[8];
@@ -402,8 +403,8 @@ __global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
     const Block8 b(jb.ne, (int)blockIdx.x - jb.blk0);
     fengine_block8<N, NT>(a, b, fsm);
 
-    uint8_t *rowbase = jb.X16 + ((size_t)b.kc * jb.nep + b.e) * 128;
-    const size_t cstride = (size_t)jb.nkc * jb.nep * 128;
+    uint8_t *rowbase = jb.X16 + ((size_t)b.kc * N * jb.nep + b.e) * 128;
+    const size_t cstride = (size_t)jb.nep * 128;
     const int pre = (b.jsub ^ (b.e & 7)) << 4, pim = ((4 + b.jsub) ^ (b.e & 7)) << 4;
     const float sc = jb.scale;
     for (int c = threadIdx.x; c < N; c += C::THREADS) {

@@ -13,13 +13,24 @@ struct FJob {
     int ne, nsp, nep, nkc;
     float scale;
     int blk0;          // first block of the job (prefix sum over the launch)
+    int wk0;           // first work item of the job in a tensor-core F-engine launch
 };
+
+// Work items of one job in a tensor-core F-engine launch (runs of 256 spectra).
+inline long fjob_tc_items(int ne, int nsp) { return (long)ne * ((nsp + 255) / 256); }
+// Whether the tensor-core F-engine handles this shape.
+inline bool fengine_tc_shape(int nch, int ntaps) { return nch == 1024 && (ntaps == 4 || ntaps == 8); }
 
 // Blocks of one job in a batched launch: 4 per (element, 32-spectrum chunk).
 inline long fjob_blocks(int ne, int nkc) { return (long)ne * nkc * 4; }
 
 mdt_status fengine_x16_batched(int nch, int ntaps, const FJob *jobs, int njobs, long nblocks,
                                cudaStream_t stream);
+// Batched tensor-core F-engine (f16 output) over jobs of Nch 1024 and one
+// Ntaps (4 or 8); `jobs` is a device array with wk0 prefix sums, `nwork` the
+// total work items.
+mdt_status fengine_tc_batched(int ntaps, const FJob *jobs, int njobs, long nwork, int *err,
+                              cudaStream_t stream);
 mdt_status check_dims(int ne, int nch, int ntaps, int nsp);
 const float2 *fft_twiddles(int n, mdt_status *st);
 

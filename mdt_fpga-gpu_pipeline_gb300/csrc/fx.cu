@@ -6,7 +6,9 @@
 // :1170) as two kernels per integration on one stream.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "mdt_common.cuh"
@@ -36,6 +38,9 @@ mdt_status xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qs
                       double2 *Vacc, int2 *raw, int *err, cudaStream_t stream);
 mdt_status channel_scales(const float2 *XB, int ne, int nch, int nsp, float target_rms, float *pw,
                           float *scales, cudaStream_t stream);
+mdt_status fengine_tc(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
+                      const int8_t *iq, const float *win, void *X16, int nep, int nkc, int ab_fmt,
+                      float scale, int *err, cudaStream_t stream);
 
 // Vacc[i] += V[i] (complex64 -> complex128), the cross-integration sum of the
 // FP32 path.
@@ -62,6 +67,7 @@ struct mdt_fx_plan_s {
     float scale = 1.0f;        // power-of-two F-output scale of the f16/bf16 path
     int *err = nullptr;        // device flag set by a timed-out wait
     double2 *acc = nullptr;    // optional FP64 cross-integration accumulator
+    bool tc_fengine = true;    // f16/bf16 path: tensor-core F-engine where it applies
     // exact int8 path: per-channel requantisation scales, calibrated from the
     // first integration's first spectra unless set by the caller
     float *qscales = nullptr, *qpower = nullptr;
@@ -192,8 +198,13 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
                              (float2 *)vis, p->acc, nullptr, p->err, p->stream);
     } else {
         const int fmt = (d.precision == MDT_PREC_BF16) ? 1 : 0;
-        st = mdt::fengine_x16(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
-                              p->window, p->X16, p->nep, p->nkc, fmt, p->scale, p->stream);
+        if (p->tc_fengine && d.nchannels == 1024 && (d.ntaps == 4 || d.ntaps == 8))
+            st = mdt::fengine_tc(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                                 p->window, p->X16, p->nep, p->nkc, fmt, p->scale, p->err,
+                                 p->stream);
+        else
+            st = mdt::fengine_x16(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                                  p->window, p->X16, p->nep, p->nkc, fmt, p->scale, p->stream);
         if (st != MDT_SUCCESS) return st;
         if (t1) cudaEventRecord(t1, p->stream);
         st = mdt::xengine_tc(d.nelements, d.nchannels, d.nspectra, p->X16, fmt, p->scale,
@@ -226,6 +237,11 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
     mdt_fx_plan p = new (std::nothrow) mdt_fx_plan_s;
     if (!p) return MDT_ERR_ALLOC;
     p->d = *desc;
+    {
+        // MDT_FENGINE=simt keeps the f16/bf16 path on the SIMT FFT F-engine
+        const char *fe = std::getenv("MDT_FENGINE");
+        p->tc_fengine = !(fe && std::string(fe) == "simt");
+    }
     const mdt_fx_desc &d = p->d;
     size_t wbytes = sizeof(float) * (size_t)d.ntaps * d.nchannels;
     size_t xbytes = 0;

@@ -59,8 +59,8 @@ constexpr size_t TC_SMEM = 1024 /*align slack*/ + (size_t)TC_STAGES * TC_STAGE_B
 
 struct TcArgs {
     const uint8_t *X;   // X16 operand base
-    long chunk_bytes;   // NEp * 128
-    long chan_bytes;    // nkc * NEp * 128
+    long chunk_bytes;   // stride between 32-spectrum chunks: Nch * NEp * 128
+    long chan_bytes;    // stride between channels: NEp * 128
     int ne, nep, nkc;
     int ntiles;
     int ab_fmt;         // 0 = f16, 1 = bf16
@@ -502,8 +502,8 @@ mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, flo
     a.ne = ne;
     a.nep = x16_padded_rows(ne);
     a.nkc = x16_chunks(nsp);
-    a.chunk_bytes = (long)a.nep * 128;
-    a.chan_bytes = (long)a.nkc * a.chunk_bytes;
+    a.chan_bytes = (long)a.nep * 128;
+    a.chunk_bytes = (long)nch * a.chan_bytes;
     a.X = (const uint8_t *)X16;
     a.ab_fmt = ab_fmt;
     a.alpha = 1.0f / ((float)nsp * scale * scale);
@@ -535,8 +535,8 @@ mdt_status xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qs
     a.ne = ne;
     a.nep = x16_padded_rows(ne);
     a.nkc = x16_chunks(nsp);
-    a.chunk_bytes = (long)a.nep * 128;
-    a.chan_bytes = (long)a.nkc * a.chunk_bytes;
+    a.chan_bytes = (long)a.nep * 128;
+    a.chunk_bytes = (long)nch * a.chan_bytes;
     a.X = (const uint8_t *)X16;
     a.ab_fmt = 0;
     a.alpha = 1.0f / (float)nsp;

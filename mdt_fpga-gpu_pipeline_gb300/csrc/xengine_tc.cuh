@@ -12,7 +12,8 @@ struct TcTile {
 // One job of a batched X-engine launch.
 struct XJob {
     const uint8_t *X;  // X16 operand of the job
-    long chunk_bytes, chan_bytes;
+    long chunk_bytes;  // stride between 32-spectrum chunks: Nch * NEp * 128
+    long chan_bytes;   // stride between channels: NEp * 128
     int ne, nep, nkc;
     float alpha;       // 1 / (Nsp * scale^2)
     float2 *V;         // visibilities [nch][ne*ne]

@@ -10,47 +10,13 @@ import pytest
 import torch
 
 from conftest import rel_fro
+from x16util import swizzle_x16, unswizzle_x16
 
 pytestmark = pytest.mark.gpu
 
 
 def dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
-
-
-def phys_index(L, e):
-    """Half-word position of logical value L (0..63) of row e in the X16 layout."""
-    return (((L >> 3) ^ (e & 7)) << 3) | (L & 7)
-
-
-def swizzle_x16(X, nep):
-    """Logical int complex X[c][s][e] (re, im ints) -> X16 bytes (f16 values)."""
-    nch, nsp, ne, _ = X.shape
-    nkc = (nsp + 31) // 32
-    rows = np.zeros((nch, nkc, nep, 64), np.float16)
-    L = np.arange(64)
-    for e in range(ne):
-        p = phys_index(L, e)
-        for kc in range(nkc):
-            s = np.arange(kc * 32, min(nsp, kc * 32 + 32))
-            vals = np.zeros((nch, 64), np.float16)
-            vals[:, :len(s)] = X[:, s, e, 0]
-            vals[:, 32:32 + len(s)] = X[:, s, e, 1]
-            rows[:, kc, e, p] = vals
-    return rows.view(np.uint8).reshape(-1)
-
-
-def unswizzle_x16(buf, nch, nsp, ne, nep):
-    nkc = (nsp + 31) // 32
-    rows = buf.view(np.float16).reshape(nch, nkc, nep, 64)
-    X = np.zeros((nch, nkc * 32, ne, 2), np.float32)
-    L = np.arange(64)
-    for e in range(ne):
-        p = phys_index(L, e)
-        logical = rows[:, :, e, :][:, :, p]  # [nch, nkc, 64]
-        X[:, :, e, 0] = logical[:, :, :32].reshape(nch, -1)
-        X[:, :, e, 1] = logical[:, :, 32:].reshape(nch, -1)
-    return X[:, :nsp]
 
 
 @pytest.mark.parametrize("ne,nch,nsp", [(40, 3, 1100), (130, 2, 600), (3, 4, 33)])
