@@ -175,6 +175,13 @@ MDT_API mdt_status mdt_fengine_tc(int ne, int nch, int ntaps, int nsp, const int
                                   const float *window, void *X16, int ab_fmt, float scale,
                                   int *err, cudaStream_t stream);
 
+/* The same tensor-core F-engine with the int8 requantisation of
+ * mdt_fengine_q8 (per-channel qscales, rint, clamp to [-127, 127]) as its
+ * output stage; the plan's INT8 precision uses it at Nch 1024. */
+MDT_API mdt_status mdt_fengine_tc_q8(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
+                                     const float *window, void *X16, const float *qscales,
+                                     int *err, cudaStream_t stream);
+
 /* Exact-int8 F-engine: as mdt_fengine_x16 but the values are integers
  * clamp(rint(x * qscales[c]), -127, 127) (stored as f16, exactly). */
 MDT_API mdt_status mdt_fengine_q8(int ne, int nch, int ntaps, int nsp, const int8_t *iq,

@@ -72,6 +72,7 @@ def _declare(L):
         "mdt_fx_set_channel_scales": ([_P, _P], _I),
         "mdt_fx_get_channel_scales": ([_P, _P], _I),
         "mdt_fengine_tc": ([_I, _I, _I, _I, _P, _P, _P, _I, _F, _P, _P], _I),
+        "mdt_fengine_tc_q8": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P], _I),
         "mdt_fengine_q8": ([_I, _I, _I, _I, _P, _P, _P, _P, _P], _I),
         "mdt_xengine_q8": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P], _I),
         "mdt_fx_integrate_static": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
@@ -303,6 +304,12 @@ def fengine_tc(ne, nch, ntaps, nsp, iq, window, X16, err, ab_fmt=0, scale=1.0, s
     """Tensor-core F-engine (Nch 1024): same output layout as fengine_x16."""
     check(lib().mdt_fengine_tc(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X16), ab_fmt, scale,
                                ptr(err), stream_handle(stream)), "fengine_tc")
+
+
+def fengine_tc_q8(ne, nch, ntaps, nsp, iq, window, X16, qscales, err, stream=None):
+    """Tensor-core F-engine with int8 requantisation (Nch 1024)."""
+    check(lib().mdt_fengine_tc_q8(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X16),
+                                  ptr(qscales), ptr(err), stream_handle(stream)), "fengine_tc_q8")
 
 
 def fengine_q8(ne, nch, ntaps, nsp, iq, window, X16, qscales, stream=None):

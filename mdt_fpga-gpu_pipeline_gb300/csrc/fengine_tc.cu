@@ -44,9 +44,10 @@ constexpr int CPT = N / GTHREADS;       // channels per thread
 constexpr int ROWB = 2 * N;             // one (spectrum, element) row of int8 I/Q
 constexpr int RUN = 256;                // spectra per work item
 constexpr uint32_t TILE = 16384;        // 128 rows x 128 bytes
-// shared memory: DFT matrix, twiddles, then per group: scaled window,
+// shared memory: DFT matrix, twiddles, int8 requantisation scales, then per
+// group: scaled window,
 // operand tiles (also the twiddled operand and the output staging), input ring
-constexpr uint32_t OFF_B = 0, OFF_TW = 8192, OFF_G = 16384;
+constexpr uint32_t OFF_B = 0, OFF_TW = 8192, OFF_QS = 16384, OFF_G = 20480;
 constexpr uint32_t G_W = 0, G_A = 32768, G_RING = 65536, G_BYTES = 98304;
 constexpr uint32_t SMEM = OFF_G + GROUPS * G_BYTES;
 // TMEM: per group 256 columns -- two 64-column MMA tiles, then 64 columns
@@ -60,6 +61,7 @@ struct Launch {
     const char2 *hist;  // first nhist spectra of the single job (may be null)
     int nhist;
     const FJob *table;  // non-null: jobs from the table, no history
+    const float *qscales;  // requantisation scales (int8 mode, single job)
     int njobs;
     int nwork;
     int *err;
@@ -141,6 +143,10 @@ __device__ __forceinline__ uint32_t lds_u32(uint32_t a)
     return v;
 }
 
+// Output modes: f16, bf16, or per-channel int8 requantisation (rint, clamp to
+// [-127, 127]) held exactly in f16 -- the operand of the exact int8 X-engine.
+enum { OUT_F16 = 0, OUT_BF16 = 1, OUT_Q8 = 2 };
+
 template <typename H>
 __device__ __forceinline__ uint32_t pack_h2(float re, float im);
 template <>
@@ -154,6 +160,20 @@ __device__ __forceinline__ uint32_t pack_h2<__nv_bfloat16>(float re, float im)
 {
     __nv_bfloat162 h = __floats2bfloat162_rn(re, im);
     return *reinterpret_cast<uint32_t *>(&h);
+}
+
+template <int MODE>
+__device__ __forceinline__ uint32_t pack_out(float re, float im, float qs)
+{
+    if constexpr (MODE == OUT_Q8) {
+        re = fminf(fmaxf(rintf(re * qs), -127.0f), 127.0f);
+        im = fminf(fmaxf(rintf(im * qs), -127.0f), 127.0f);
+        return pack_h2<__half>(re, im);
+    } else if constexpr (MODE == OUT_BF16) {
+        return pack_h2<__nv_bfloat16>(re, im);
+    } else {
+        return pack_h2<__half>(re, im);
+    }
 }
 
 // Channel of slot q (0..31: q = 8 * j + warp) for lane l.  The map is a
@@ -175,7 +195,7 @@ __device__ __forceinline__ uint32_t tile_word(int r, int w)
     return (uint32_t)r * 128u + ((uint32_t)((w >> 2) ^ (r & 7)) << 4) + ((uint32_t)(w & 3) << 2);
 }
 
-template <int NT, typename H>
+template <int NT, int MODE>
 __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
 {
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -211,6 +231,9 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
         sincospif((float)(k1 * n2) / 512.0f, &s, &c);
         tw[i] = make_float2(c, -s);
     }
+    float *qs_s = reinterpret_cast<float *>(sm + OFF_QS);
+    if constexpr (MODE == OUT_Q8)
+        for (int i = tid; i < N; i += THREADS) qs_s[i] = __ldg(L.qscales + i);
     if (tid == 0) {
         for (int gg = 0; gg < GROUPS; gg++)
             for (int b = 0; b < 3; b++) tc::mbar_init(tc::smem_u32(&bars[gg][b]), 1);
@@ -447,8 +470,10 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
 #pragma unroll
                     for (int kk = 0; kk < 16; kk++) {
                         const int c = l + 32 * (half * 16 + kk);
+                        const float qs = MODE == OUT_Q8 ? qs_s[c] : 1.0f;
                         sts_u32(gA + (uint32_t)(c * 32) + (uint32_t)((su ^ ((c >> 2) & 7)) << 2),
-                                pack_h2<H>(__uint_as_float(v[2 * kk]), __uint_as_float(v[2 * kk + 1])));
+                                pack_out<MODE>(__uint_as_float(v[2 * kk]),
+                                               __uint_as_float(v[2 * kk + 1]), qs));
                     }
                 }
             }
@@ -530,7 +555,7 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
 
 }  // namespace ftc
 
-static mdt_status launch_tc(int ntaps, int ab_fmt, const ftc::Launch &L, cudaStream_t stream)
+static mdt_status launch_tc(int ntaps, int mode, const ftc::Launch &L, cudaStream_t stream)
 {
     int dev = 0, nsm = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -544,18 +569,23 @@ static mdt_status launch_tc(int ntaps, int ab_fmt, const ftc::Launch &L, cudaStr
         kern<<<(unsigned)blocks, ftc::THREADS, ftc::SMEM, stream>>>(L);
         return launch_status("fengine_tc_kernel");
     };
+    using namespace ftc;
     if (ntaps == 8)
-        return ab_fmt ? launch(ftc::fengine_tc_kernel<8, __nv_bfloat16>)
-                      : launch(ftc::fengine_tc_kernel<8, __half>);
-    return ab_fmt ? launch(ftc::fengine_tc_kernel<4, __nv_bfloat16>)
-                  : launch(ftc::fengine_tc_kernel<4, __half>);
+        return mode == OUT_Q8 ? launch(fengine_tc_kernel<8, OUT_Q8>)
+             : mode == OUT_BF16 ? launch(fengine_tc_kernel<8, OUT_BF16>)
+                                : launch(fengine_tc_kernel<8, OUT_F16>);
+    return mode == OUT_Q8 ? launch(fengine_tc_kernel<4, OUT_Q8>)
+         : mode == OUT_BF16 ? launch(fengine_tc_kernel<4, OUT_BF16>)
+                            : launch(fengine_tc_kernel<4, OUT_F16>);
 }
 
 // Tensor-core F-engine, Nch = 1024, Ntaps 4 or 8.  `err` (device int) is set
-// to 1 if a wait timed out.  Same arguments and output as fengine_x16.
+// to 1 if a wait timed out.  Same arguments and output as fengine_x16, or,
+// with `qscales`, as fengine_q8 (int8 requantisation, `scale` and `ab_fmt`
+// unused).
 mdt_status fengine_tc(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
                       const int8_t *iq, const float *win, void *X16, int nep, int nkc, int ab_fmt,
-                      float scale, int *err, cudaStream_t stream)
+                      float scale, int *err, cudaStream_t stream, const float *qscales)
 {
     if (!fengine_tc_shape(nch, ntaps))
         return invalid("fengine_tc: needs Nch = 1024 and Ntaps 4 or 8");
@@ -573,7 +603,7 @@ mdt_status fengine_tc(int ne, int nch, int ntaps, int nsp, const int8_t *hist, i
     L.one.nsp = nsp;
     L.one.nep = nep;
     L.one.nkc = nkc;
-    L.one.scale = scale;
+    L.one.scale = qscales ? 1.0f : scale;
     L.one.blk0 = 0;
     L.one.wk0 = 0;
     L.hist = reinterpret_cast<const char2 *>(hist);
@@ -582,7 +612,9 @@ mdt_status fengine_tc(int ne, int nch, int ntaps, int nsp, const int8_t *hist, i
     L.njobs = 1;
     L.nwork = (int)nwork;
     L.err = err;
-    return launch_tc(ntaps, ab_fmt, L, stream);
+    L.qscales = qscales;
+    return launch_tc(ntaps, qscales ? ftc::OUT_Q8 : (ab_fmt ? ftc::OUT_BF16 : ftc::OUT_F16), L,
+                     stream);
 }
 
 mdt_status fengine_tc_batched(int ntaps, const FJob *jobs, int njobs, long nwork, int *err,
@@ -596,7 +628,7 @@ mdt_status fengine_tc_batched(int ntaps, const FJob *jobs, int njobs, long nwork
     L.njobs = njobs;
     L.nwork = (int)nwork;
     L.err = err;
-    return launch_tc(ntaps, 0, L, stream);
+    return launch_tc(ntaps, ftc::OUT_F16, L, stream);
 }
 
 }  // namespace mdt
@@ -609,5 +641,16 @@ extern "C" MDT_API mdt_status mdt_fengine_tc(int ne, int nch, int ntaps, int nsp
     if (!(scale > 0.0f)) return mdt::invalid("fengine_tc: scale must be positive");
     const int nep = (ne + 15) / 16 * 16, nkc = (nsp + 31) / 32;
     return mdt::fengine_tc(ne, nch, ntaps, nsp, nullptr, 0, iq, window, X16, nep, nkc, ab_fmt,
-                           scale, err, stream);
+                           scale, err, stream, nullptr);
+}
+
+extern "C" MDT_API mdt_status mdt_fengine_tc_q8(int ne, int nch, int ntaps, int nsp,
+                                                const int8_t *iq, const float *window, void *X16,
+                                                const float *qscales, int *err,
+                                                cudaStream_t stream)
+{
+    if (!qscales) return mdt::invalid("fengine_tc_q8: null scales");
+    const int nep = (ne + 15) / 16 * 16, nkc = (nsp + 31) / 32;
+    return mdt::fengine_tc(ne, nch, ntaps, nsp, nullptr, 0, iq, window, X16, nep, nkc, 0, 1.0f,
+                           err, stream, qscales);
 }

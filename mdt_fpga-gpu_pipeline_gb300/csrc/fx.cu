@@ -40,7 +40,7 @@ mdt_status channel_scales(const float2 *XB, int ne, int nch, int nsp, float targ
                           float *scales, cudaStream_t stream);
 mdt_status fengine_tc(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
                       const int8_t *iq, const float *win, void *X16, int nep, int nkc, int ab_fmt,
-                      float scale, int *err, cudaStream_t stream);
+                      float scale, int *err, cudaStream_t stream, const float *qscales);
 
 // Vacc[i] += V[i] (complex64 -> complex128), the cross-integration sum of the
 // FP32 path.
@@ -190,8 +190,13 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
             if (st != MDT_SUCCESS) return st;
             p->qscales_valid = true;
         }
-        st = mdt::fengine_q8(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
-                             p->window, p->X16, p->nep, p->nkc, p->qscales, p->stream);
+        if (p->tc_fengine && d.nchannels == 1024 && (d.ntaps == 4 || d.ntaps == 8))
+            st = mdt::fengine_tc(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                                 p->window, p->X16, p->nep, p->nkc, 0, 1.0f, p->err, p->stream,
+                                 p->qscales);
+        else
+            st = mdt::fengine_q8(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
+                                 p->window, p->X16, p->nep, p->nkc, p->qscales, p->stream);
         if (st != MDT_SUCCESS) return st;
         if (t1) cudaEventRecord(t1, p->stream);
         st = mdt::xengine_q8(d.nelements, d.nchannels, d.nspectra, p->X16, p->qscales,
@@ -201,7 +206,7 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
         if (p->tc_fengine && d.nchannels == 1024 && (d.ntaps == 4 || d.ntaps == 8))
             st = mdt::fengine_tc(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
                                  p->window, p->X16, p->nep, p->nkc, fmt, p->scale, p->err,
-                                 p->stream);
+                                 p->stream, nullptr);
         else
             st = mdt::fengine_x16(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
                                   p->window, p->X16, p->nep, p->nkc, fmt, p->scale, p->stream);

@@ -89,3 +89,64 @@ def test_plan_fp16_uses_tensor_core_fengine(mdt, cuda, oracle):
         print("integration %d: max channel rel err %.2e" % (j, e))
         assert e < 1e-3
     plan.close()
+
+
+def test_fengine_tc_q8_within_one_lsb(mdt, cuda, oracle):
+    """int8 requantisation on the tensor-core F-engine: within 1 LSB of the
+    FP64 F-output quantised with the same scales (the f16 DFT moves values
+    that sit within ~0.01 LSB of a rounding boundary)."""
+    ne, nch, ntaps, nsp = 6, 1024, 8, 96
+    iq = oracle.synth_iq(77, ne, nch, 0, nsp + ntaps - 1, np.full(ne, 16 * 256, np.int32))
+    win = oracle.window_hamming_sinc(nch, ntaps)
+    F = fp64_fout(oracle, iq, win, ne, nch, ntaps, nsp)           # [s][e][c]
+    rms = np.sqrt(np.mean(np.abs(F) ** 2, axis=(0, 1)))
+    qs = (20.0 / rms).astype(np.float32)
+    want_re = np.clip(np.rint(F.real * qs.astype(np.float64)), -127, 127)
+    want_im = np.clip(np.rint(F.imag * qs.astype(np.float64)), -127, 127)
+    nep = (ne + 15) // 16 * 16
+    X16 = torch.zeros(mdt.x16_bytes(ne, nch, nsp), dtype=torch.uint8, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    mdt.fengine_tc_q8(ne, nch, ntaps, nsp, dev(iq), dev(win), X16, dev(qs), err)
+    torch.cuda.synchronize()
+    assert err.item() == 0
+    got = unswizzle_x16(X16.cpu().numpy(), nch, nsp, ne, nep)
+    gre = np.transpose(got[..., 0], (1, 2, 0))
+    gim = np.transpose(got[..., 1], (1, 2, 0))
+    assert np.all(gre == np.rint(gre)) and np.all(np.abs(gre) <= 127)
+    d = np.maximum(np.abs(gre - want_re), np.abs(gim - want_im))
+    print("int8 F-output: %.4f of values exact" % np.mean(d == 0))
+    assert d.max() <= 1
+    assert np.mean(d == 0) > 0.97
+
+
+def test_plan_int8_at_1024_channels(mdt, cuda, oracle):
+    """The plan's INT8 path at Nch = 1024 runs the tensor-core F-engine with
+    requantisation: identical to the stages called directly with its scales,
+    and within the int8 quantisation error of FP64."""
+    cfg = mdt.configs.small(mdt.configs.C3, nelements=20, nchannels=1024, nspectra=256)
+    ne, nch, ntaps, nsp = cfg.nelements, cfg.nchannels, cfg.ntaps, cfg.nspectra
+    ssig, sdel = cfg.sources()
+    iq_h = oracle.synth_iq(cfg.seed, ne, nch, 0, nsp + ntaps - 1, cfg.sigma_q8(), None, ssig, sdel)
+    iq = dev(iq_h)
+    win = dev(oracle.window_hamming_sinc(nch, ntaps))
+    plan = mdt.FxPlan(ne, nch, ntaps, nsp, precision=mdt.MDT_PREC_INT8)
+    plan.set_window(win)
+    vis = torch.empty(nch, ne, ne, dtype=torch.complex64, device="cuda")
+    plan.execute(iq, 1, vis)
+    plan.check()
+    qs = torch.empty(nch, dtype=torch.float32, device="cuda")
+    plan.get_channel_scales(qs)
+    X16 = torch.zeros(mdt.x16_bytes(ne, nch, nsp), dtype=torch.uint8, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    mdt.fengine_tc_q8(ne, nch, ntaps, nsp, iq, win, X16, qs, err)
+    v2 = torch.empty_like(vis)
+    mdt.xengine_q8(ne, nch, nsp, X16, qs, vis=v2, err=err)
+    torch.cuda.synchronize()
+    assert err.item() == 0
+    assert torch.equal(v2.view(torch.int64), vis.view(torch.int64))
+    sel = [0, 7, 511, 1023]
+    ref = oracle.fx(iq_h, win.cpu().numpy(), ne, nch, ntaps, nsp, channels=sel)
+    e = max(rel(vis.cpu().numpy()[k], ref[i]) for i, k in enumerate(sel))
+    print("int8 plan at 1024 channels: max channel rel err %.3e" % e)
+    assert e < 2e-2
+    plan.close()
