@@ -43,6 +43,12 @@ sys.path.insert(0, ROOT)
 # same integration, so no scaling is needed.
 NCU_TRAFFIC = {"fengine_c64b": 672.395008e6 + 2631.648e6,
                "xengine_herm_f32": 2685.021e6 + 27.394048e6}
+# The tensor path's kernels on one c3 integration (Nsp = 8192), scaled from ncu
+# captures at Nsp = 1024 (profiles/fengine_tc_c3.txt, profiles/xengine_tc_c3.txt):
+# the F-engine's reads and writes and the X-engine's operand reads grow with
+# the spectra processed, the X-engine's visibility writes do not.
+NCU_TRAFFIC_C3 = {"fengine_tc": 0.554507e9 * 8199 / 1031 + 1.032375e9 * 8,
+                  "xengine_tc": 1.074186e9 * 8 + 0.493379e9}
 
 
 def load_pkg():
@@ -241,28 +247,48 @@ def measure_plan(mdt, cfg, precision, dev, steps, warmup, seed_offset=0):
 
 def tensor_path_section(mdt, dev, steps):
     """c3_array256 (NE=256, Nch=1024, Ntaps=8, Nsp=8192): the f16 tensor-core
-    path over the full 8 integrations and the plain FP32 path over one
-    integration, in antenna-samples/s, with the tensor X-engine's TFLOP/s."""
+    path (tensor-core F-engine + tensor-core X-engine) over the full 8
+    integrations, the exact int8 path over the same, and the plain FP32 path
+    and the SIMT-FFT f16 F-engine over one integration, in antenna-samples/s,
+    with each kernel's roofline."""
     c3 = mdt.configs.C3
     hbm, bf16, kind = peaks()
     ms16, f16, x16, scale = measure_plan(mdt, c3, 1, dev, steps=steps, warmup=1)
+    ms8, f8, x8, _ = measure_plan(mdt, c3, 3, dev, steps=max(1, steps // 2), warmup=1)
     c3_one = mdt.configs.small(c3, nint=1)
     ms32, f32, x32, _ = measure_plan(mdt, c3_one, 0, dev, steps=1, warmup=1)
+    os.environ["MDT_FENGINE"] = "simt"
+    try:
+        _, fsimt, _, _ = measure_plan(mdt, c3_one, 1, dev, steps=1, warmup=1)
+    finally:
+        del os.environ["MDT_FENGINE"]
     ne, nch, nsp, ntaps = c3.nelements, c3.nchannels, c3.nspectra, c3.ntaps
     flops = 8.0 * ne * (ne + 1) / 2 * nsp * nch
     v16 = c3.antenna_samples() / (ms16 * 1e-3)
+    v8 = c3.antenna_samples() / (ms8 * 1e-3)
     v32 = c3_one.antenna_samples() / (ms32 * 1e-3)
     x_tflops = flops / (x16 * 1e-3) / 1e12
     f_bytes = (nsp + ntaps - 1) * ne * nch * 2 + nch * ((nsp + 31) // 32) * ((ne + 15) // 16 * 16) * 128
+
+    def fe(ms, traffic=None):
+        gbs = f_bytes / (ms * 1e-3) / 1e9
+        return {"ms_per_launch": ms, "gbs": gbs, "frac": gbs / hbm, "bound": "hbm",
+                "algorithmic_bytes": f_bytes, "peak_source": kind + " hbm_gbs",
+                "traffic": traffic}
+
     return {
         "workload": c3.name, "precision": "f16 operands, fp32 accumulate (tcgen05 kind::f16)",
         "value": v16, "unit": "antenna-samples/s", "ms_per_step": ms16,
         "integrations": c3.nint, "fp32_path_value": v32, "speedup_vs_fp32_path": v16 / v32,
         "xengine_tc": {"ms_per_launch": x16, "tflops": x_tflops, "peak": bf16,
                        "frac": x_tflops / bf16, "peak_source": kind + " bf16_tflops (dense)",
-                       "algorithmic_flops": flops},
-        "fengine_x16": {"ms_per_launch": f16, "gbs": f_bytes / (f16 * 1e-3) / 1e9,
-                        "frac": f_bytes / (f16 * 1e-3) / 1e9 / hbm, "algorithmic_bytes": f_bytes},
+                       "algorithmic_flops": flops, "traffic": NCU_TRAFFIC_C3["xengine_tc"]},
+        "fengine_tc": fe(f16, NCU_TRAFFIC_C3["fengine_tc"]),
+        "fengine_simt_fft": fe(fsimt),
+        "int8_path": {"value": v8, "unit": "antenna-samples/s", "ms_per_step": ms8,
+                      "speedup_vs_fp32_path": v8 / v32, "fengine_ms": f8, "xengine_ms": x8,
+                      "precision": "int8 F-output, exact int32 sums (f16 MMAs over FP32-exact "
+                                   "windows)"},
         "fp32_path": {"fengine_ms": f32, "xengine_ms": x32},
         "f16_scale": scale,
     }
