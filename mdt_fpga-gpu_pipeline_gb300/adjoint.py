@@ -148,6 +148,7 @@ def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9,
             callback(len(hist), hist[-1])
         if hist[-1][0] < tol:
             break
-        h = torch.einsum("cb,cab->ca", g.abs() ** 2, m2)  # model is Hermitian
+        gg = g.real ** 2 + g.imag ** 2
+        h = (m2 * gg[:, None, :]).sum(dim=2)  # model is Hermitian: |M_ab| = |M_ba|
         g = g - step * gv.grad.to(torch.complex128) / (2 * h)
     return g.to(torch.complex64), hist

@@ -149,6 +149,34 @@ __global__ void pfb_tap_grad_partial_kernel(int nch, int ntaps, int ne, int nsp,
     part[((long)p * ntaps + i) * nch + k] = acc;
 }
 
+// All taps at once (Ntaps <= 16): gP is read once, the int8 input of the
+// NT taps from L2.  part[p][i][k] as above.
+template <int NT>
+__global__ void pfb_tap_grad_all_kernel(int nch, int ne, int nsp, int nsplit,
+                                        const float2 *__restrict__ gP,
+                                        const char2 *__restrict__ iq, double *__restrict__ part)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.y;
+    if (k >= nch) return;
+    const long rows = (long)nsp * ne;
+    const long r0 = rows * p / nsplit, r1 = rows * (p + 1) / nsplit;
+    double acc[NT];
+#pragma unroll
+    for (int i = 0; i < NT; i++) acc[i] = 0.0;
+    for (long row = r0; row < r1; row++) {
+        const long s = row / ne, e = row - s * ne;
+        const float2 g = gP[row * nch + k];
+#pragma unroll
+        for (int i = 0; i < NT; i++) {
+            const char2 x = iq[((s + i) * ne + e) * nch + k];
+            acc[i] += (double)g.x * (double)x.x + (double)g.y * (double)x.y;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NT; i++) part[((long)p * NT + i) * nch + k] = acc[i];
+}
+
 // gW[i][k] = sum_p part[p][i][k] in increasing p (deterministic).
 __global__ void pfb_tap_grad_reduce_kernel(int n, int nsplit, const double *__restrict__ part,
                                            float *__restrict__ gW)
@@ -221,11 +249,23 @@ MDT_API mdt_status mdt_pfb_tap_grad(int ne, int nch, int ntaps, int nsp, const v
     int nsplit = (int)std::min<long>(64, std::max<long>(1, workspace_bytes / (sizeof(double) * n)));
     if (nsplit < 1 || workspace_bytes < sizeof(double) * n)
         return mdt::invalid("pfb_tap_grad: workspace must hold Ntaps*Nch doubles");
-    dim3 grid((unsigned)mdt::cdiv(nch, 128), (unsigned)ntaps, (unsigned)nsplit);
-    mdt::pfb_tap_grad_partial_kernel<<<grid, 128, 0, stream>>>(
-        nch, ntaps, ne, nsp, nsplit, (const float2 *)gradP, (const char2 *)iq,
-        (double *)workspace);
-    mdt_status st = mdt::launch_status("pfb_tap_grad_partial_kernel");
+    mdt_status st;
+    if (ntaps == 4 || ntaps == 8) {
+        dim3 grid((unsigned)mdt::cdiv(nch, 128), (unsigned)nsplit);
+        if (ntaps == 4)
+            mdt::pfb_tap_grad_all_kernel<4><<<grid, 128, 0, stream>>>(
+                nch, ne, nsp, nsplit, (const float2 *)gradP, (const char2 *)iq, (double *)workspace);
+        else
+            mdt::pfb_tap_grad_all_kernel<8><<<grid, 128, 0, stream>>>(
+                nch, ne, nsp, nsplit, (const float2 *)gradP, (const char2 *)iq, (double *)workspace);
+        st = mdt::launch_status("pfb_tap_grad_all_kernel");
+    } else {
+        dim3 grid((unsigned)mdt::cdiv(nch, 128), (unsigned)ntaps, (unsigned)nsplit);
+        mdt::pfb_tap_grad_partial_kernel<<<grid, 128, 0, stream>>>(
+            nch, ntaps, ne, nsp, nsplit, (const float2 *)gradP, (const char2 *)iq,
+            (double *)workspace);
+        st = mdt::launch_status("pfb_tap_grad_partial_kernel");
+    }
     if (st != MDT_SUCCESS) return st;
     mdt::pfb_tap_grad_reduce_kernel<<<(unsigned)mdt::cdiv(n, 256), 256, 0, stream>>>(
         (int)n, nsplit, (const double *)workspace, gradW);
