@@ -40,6 +40,8 @@
 // the MMAs and commits; warps 2-5 read the accumulators (one TMEM lane
 // quarter each) and write visibilities.  Every mbarrier wait is bounded; a
 // timeout sets the error flag and the block finishes without further work.
+#include <cstdlib>
+
 #include "mdt_common.cuh"
 #include "tc_ptx.cuh"
 #include "xengine_tc.cuh"
@@ -55,6 +57,11 @@ constexpr uint32_t TC_B_BYTES = TC_BROWS * 128;
 constexpr uint32_t TC_A_BYTES = TC_AROWS * 128;
 constexpr uint32_t TC_STAGE_BYTES = TC_B_BYTES + TC_A_BYTES;
 constexpr size_t TC_SMEM = 1024 /*align slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES + 256;
+// shared memory of the single-launch kernel for a (BROWS, STAGES) shape
+constexpr size_t tc_smem(int brows, int stages)
+{
+    return 1024 + (size_t)stages * ((size_t)brows * 128 + TC_A_BYTES) + 256;
+}
 
 
 struct TcArgs {
@@ -75,18 +82,24 @@ struct TcArgs {
 
 constexpr int TC_WIN = 16;  // K-chunks (of 32 spectra) per exact accumulation window
 
-template <int KIND>  // 0: f16 / bf16 operands, float results; 1: exact int8-valued f16
-__global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_constant__ TcArgs a)
+// STAGES-deep ring of (B: BROWS rows, A: 128 rows) stages; BROWS 256 with 4
+// stages (one block per SM) or 128 with 3 stages (two blocks per SM, so one
+// block's epilogue overlaps the other's products).
+template <int KIND, int BROWS, int STAGES>  // KIND 0: f16 / bf16, float results; 1: exact int8
+__global__ void __launch_bounds__(TC_THREADS, (BROWS == 128 ? 2 : 1))
+    xengine_tc_kernel(const __grid_constant__ TcArgs a)
 {
+    constexpr uint32_t B_BYTES = BROWS * 128;
+    constexpr uint32_t STAGE_BYTES = B_BYTES + TC_A_BYTES;
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *bars = (uint64_t *)(smem + (size_t)TC_STAGES * TC_STAGE_BYTES);
+    uint64_t *bars = (uint64_t *)(smem + (size_t)STAGES * STAGE_BYTES);
     // bars[0..S) full, bars[S..2S) empty, bars[2S] done, bars[2S+1..2S+2] window
     // full, bars[2S+3..2S+4] window empty; then the TMEM address slot
-    uint64_t *win_full = bars + 2 * TC_STAGES + 1;
-    uint64_t *win_empty = bars + 2 * TC_STAGES + 3;
-    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 5);
+    uint64_t *win_full = bars + 2 * STAGES + 1;
+    uint64_t *win_empty = bars + 2 * STAGES + 3;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * STAGES + 5);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = blockIdx.x / a.ntiles;
@@ -97,7 +110,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
                          : (NCOLMUL * N <= 128) ? 128 : (NCOLMUL * N <= 256) ? 256 : 512;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < 2 * TC_STAGES + 3; s++) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
+        for (int s = 0; s < 2 * STAGES + 3; s++) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
         tc::mbar_init(tc::smem_u32(&win_empty[0]), 4);  // one arrival per epilogue warp
         tc::mbar_init(tc::smem_u32(&win_empty[1]), 4);
         tc::fence_mbar_init();
@@ -121,26 +134,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
         const int arows = min(TC_AROWS, a.nep - tile.r0);
         const uint32_t abytes = tile.a_sep ? (uint32_t)arows * 128 : 0;
         for (int kc = 0; kc < a.nkc && ok; kc++) {
-            const int s = kc % TC_STAGES;
-            if (kc >= TC_STAGES) {
-                ok = tc::mbar_wait(tc::smem_u32(&bars[TC_STAGES + s]), ((kc / TC_STAGES) - 1) & 1);
+            const int s = kc % STAGES;
+            if (kc >= STAGES) {
+                ok = tc::mbar_wait(tc::smem_u32(&bars[STAGES + s]), ((kc / STAGES) - 1) & 1);
                 if (!ok) break;
             }
-            uint8_t *stage = smem + (size_t)s * TC_STAGE_BYTES;
+            uint8_t *stage = smem + (size_t)s * STAGE_BYTES;
             const uint32_t full = tc::smem_u32(&bars[s]);
             tc::mbar_expect_tx(full, bbytes + abytes);
             const uint8_t *src = xc + (long)kc * a.chunk_bytes;
             tc::bulk_g2s(tc::smem_u32(stage), src + (long)tile.q0 * 128, bbytes, full);
             if (abytes)
-                tc::bulk_g2s(tc::smem_u32(stage + TC_B_BYTES), src + (long)tile.r0 * 128, abytes,
+                tc::bulk_g2s(tc::smem_u32(stage + B_BYTES), src + (long)tile.r0 * 128, abytes,
                              full);
         }
         // drain: wait until the MMAs consumed every issued stage, so no copy
         // is in flight when the block exits
         if (ok) {
-            for (int kc = max(0, a.nkc - TC_STAGES); kc < a.nkc && ok; kc++)
-                ok = tc::mbar_wait(tc::smem_u32(&bars[TC_STAGES + (kc % TC_STAGES)]),
-                                   (kc / TC_STAGES) & 1);
+            for (int kc = max(0, a.nkc - STAGES); kc < a.nkc && ok; kc++)
+                ok = tc::mbar_wait(tc::smem_u32(&bars[STAGES + (kc % STAGES)]),
+                                   (kc / STAGES) & 1);
         }
         if (!ok) atomicExch(a.err, 1);
     } else if (warp == 1 && lane == 0) {
@@ -148,7 +161,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
         const uint32_t id_pos = tc::idesc_f16(N, a.ab_fmt, 0);
         const uint32_t id_neg = tc::idesc_f16(N, a.ab_fmt, 1);
         for (int kc = 0; kc < a.nkc && ok; kc++) {
-            const int s = kc % TC_STAGES;
+            const int s = kc % STAGES;
             uint32_t acc_re = d_re, acc_im = d_im;
             bool first = (kc == 0);
             if constexpr (KIND == 1) {
@@ -162,11 +175,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
                 acc_re = tmem + (uint32_t)(h * 2 * N);
                 acc_im = acc_re + (uint32_t)N;
             }
-            ok = tc::mbar_wait(tc::smem_u32(&bars[s]), (kc / TC_STAGES) & 1);
+            ok = tc::mbar_wait(tc::smem_u32(&bars[s]), (kc / STAGES) & 1);
             if (!ok) break;
             tc::fence_after_sync();
-            const uint32_t sb = tc::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
-            const uint32_t sa = tile.a_sep ? sb + TC_B_BYTES : sb + (uint32_t)(tile.r0 - tile.q0) * 128;
+            const uint32_t sb = tc::smem_u32(smem + (size_t)s * STAGE_BYTES);
+            const uint32_t sa = tile.a_sep ? sb + B_BYTES : sb + (uint32_t)(tile.r0 - tile.q0) * 128;
             const uint64_t bd = tc::sw128_kmajor_desc(sb);
             const uint64_t ad = tc::sw128_kmajor_desc(sa);
             // k-step j advances the start address by 32 bytes (+2 in the >>4 field)
@@ -178,13 +191,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
             tc::mma_f16(acc_im, ad + 6, bd + 2, id_pos, 1);
             tc::mma_f16(acc_im, ad + 0, bd + 4, id_neg, 1);
             tc::mma_f16(acc_im, ad + 2, bd + 6, id_neg, 1);
-            tc::mma_commit(tc::smem_u32(&bars[TC_STAGES + s]));
+            tc::mma_commit(tc::smem_u32(&bars[STAGES + s]));
             if constexpr (KIND == 1) {
                 if ((kc % TC_WIN) == TC_WIN - 1 || kc == a.nkc - 1)
                     tc::mma_commit(tc::smem_u32(&win_full[(kc / TC_WIN) & 1]));
             }
         }
-        tc::mma_commit(tc::smem_u32(&bars[2 * TC_STAGES]));
+        tc::mma_commit(tc::smem_u32(&bars[2 * STAGES]));
         if (!ok) atomicExch(a.err, 1);
     } else if (warp >= 2 && KIND == 1) {
         // ---------------- epilogue, exact int8 mode: fold windows into int32
@@ -260,39 +273,61 @@ __global__ void __launch_bounds__(TC_THREADS, 1) xengine_tc_kernel(const __grid_
         if (!ok && lane == 0) atomicExch(a.err, 1);
     } else if (warp >= 2 && KIND == 0) {
         // ---------------- epilogue: TMEM -> visibilities
-        ok = tc::mbar_wait_sleep(tc::smem_u32(&bars[2 * TC_STAGES]), 0);
+        ok = tc::mbar_wait_sleep(tc::smem_u32(&bars[2 * STAGES]), 0);
         tc::fence_after_sync();
         const int quarter = warp & 3;
         const int r = tile.r0 + quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
         float2 *Vc = a.V ? a.V + (long)ch * a.ne * a.ne : nullptr;
         double2 *Ac = a.Vacc ? a.Vacc + (long)ch * a.ne * a.ne : nullptr;
-        for (int n0 = 0; n0 < N; n0 += 16) {
-            uint32_t vr[16], vi[16];
-            tc::tmem_ld16(d_re + lane_off + n0, vr);
-            tc::tmem_ld16(d_im + lane_off + n0, vi);
-            tc::tmem_ld_wait();
-            if (!ok || r >= a.ne) continue;
+        // The lower triangle V[q*NE + r] is written along r (the lanes).  The
+        // conjugate mirror V[r*NE + q] is transposed through shared memory (the
+        // stage ring is idle once every MMA has completed) in 32 x 32 blocks
+        // so that it is written along q as well.
+        float2 *tb = reinterpret_cast<float2 *>(smem) + (size_t)quarter * 32 * 33;  // [q][r]
+        const int rbase = tile.r0 + quarter * 32;
+        for (int n0 = 0; n0 < N; n0 += 32) {
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int q = tile.q0 + n0 + j;
-                if (q >= a.ne || q > r) continue;
-                const float re = __uint_as_float(vr[j]) * a.alpha;
-                const float im = (q == r) ? 0.0f : __uint_as_float(vi[j]) * a.alpha;
-                const long lo = (long)q * a.ne + r, up = (long)r * a.ne + q;
-                if (Vc) {
-                    Vc[lo] = make_float2(re, im);
-                    if (q != r) Vc[up] = make_float2(re, -im);
+            for (int h = 0; h < 2; h++) {
+                uint32_t vr[16], vi[16];
+                const bool has = n0 + 16 * h < N;
+                if (has) {
+                    tc::tmem_ld16(d_re + lane_off + n0 + 16 * h, vr);
+                    tc::tmem_ld16(d_im + lane_off + n0 + 16 * h, vi);
+                    tc::tmem_ld_wait();
                 }
-                if (Ac) {
-                    double2 x = Ac[lo];
-                    Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
-                    if (q != r) {
-                        double2 y = Ac[up];
-                        Ac[up] = make_double2(y.x + (double)re, y.y - (double)im);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int q = tile.q0 + n0 + 16 * h + j;
+                    const bool live = has && ok && r < a.ne && q < a.ne && q <= r;
+                    const float re = live ? __uint_as_float(vr[j]) * a.alpha : 0.0f;
+                    const float im = (live && q != r) ? __uint_as_float(vi[j]) * a.alpha : 0.0f;
+                    tb[(16 * h + j) * 33 + lane] = make_float2(re, -im);
+                    if (!live) continue;
+                    const long lo = (long)q * a.ne + r;
+                    if (Vc) Vc[lo] = make_float2(re, im);
+                    if (Ac) {
+                        double2 x = Ac[lo];
+                        Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
                     }
                 }
             }
+            __syncwarp();
+            // mirror: row r = rbase + rr, columns q = tile.q0 + n0 + lane (q < r)
+            const int q = tile.q0 + n0 + lane;
+#pragma unroll 4
+            for (int rr = 0; rr < 32; rr++) {
+                const int rm = rbase + rr;
+                if (!ok || rm >= a.ne || q >= a.ne || q >= rm || n0 + lane >= N) continue;
+                const float2 v = tb[lane * 33 + rr];
+                const long up = (long)rm * a.ne + q;
+                if (Vc) Vc[up] = v;
+                if (Ac) {
+                    double2 y = Ac[up];
+                    Ac[up] = make_double2(y.x + (double)v.x, y.y + (double)v.y);
+                }
+            }
+            __syncwarp();
         }
         if (!ok && lane == 0) atomicExch(a.err, 1);
         tc::fence_before_sync();
@@ -512,15 +547,26 @@ mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, flo
     a.err = err;
     a.qscales = nullptr;
     a.raw = nullptr;
-    a.ntiles = make_tiles(ne, a.nep, TC_BROWS, a.tiles);
+    // column chunks of <= 128 with a 3-stage ring: two blocks per SM;
+    // MDT_XTILE=256 selects <= 256-wide chunks, 4 stages, one block per SM
+    static const bool wide = [] {
+        const char *v = getenv("MDT_XTILE");
+        return v && atoi(v) == 256;
+    }();
+    const int maxw = wide ? 256 : 128;
+    a.ntiles = make_tiles(ne, a.nep, maxw, a.tiles);
     if (a.ntiles <= 0) return invalid("xengine_tc: too many tiles");
-    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<0>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-    if (e != cudaSuccess) return cuda_status(e, "xengine_tc smem attribute");
     long blocks = (long)nch * a.ntiles;
     if (blocks > 0x7fffffffL) return invalid("xengine_tc: grid too large");
-    xengine_tc_kernel<0><<<(unsigned)blocks, TC_THREADS, TC_SMEM, stream>>>(a);
-    return launch_status("xengine_tc_kernel");
+    auto launch = [&](auto kern, size_t smem) -> mdt_status {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return cuda_status(e, "xengine_tc smem attribute");
+        kern<<<(unsigned)blocks, TC_THREADS, smem, stream>>>(a);
+        return launch_status("xengine_tc_kernel");
+    };
+    return wide ? launch(xengine_tc_kernel<0, 256, 4>, tc_smem(256, 4))
+                : launch(xengine_tc_kernel<0, 128, 3>, tc_smem(128, 3));
 }
 
 // Exact int8 mode: X16 holds integers in [-127, 127] (f16) requantised with
@@ -547,12 +593,13 @@ mdt_status xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qs
     a.raw = raw;
     a.ntiles = make_tiles(ne, a.nep, 64, a.tiles);
     if (a.ntiles <= 0) return invalid("xengine_q8: too many tiles");
-    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<1>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<1, 256, 4>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tc_smem(256, 4));
     if (e != cudaSuccess) return cuda_status(e, "xengine_q8 smem attribute");
     long blocks = (long)nch * a.ntiles;
     if (blocks > 0x7fffffffL) return invalid("xengine_q8: grid too large");
-    xengine_tc_kernel<1><<<(unsigned)blocks, TC_THREADS, TC_SMEM, stream>>>(a);
+    xengine_tc_kernel<1, 256, 4><<<(unsigned)blocks, TC_THREADS, tc_smem(256, 4), stream>>>(a);
     return launch_status("xengine_tc_kernel<exact int8>");
 }
 
