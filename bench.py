@@ -380,6 +380,10 @@ def gaincal_section(mdt, dev, steps):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    # warm-up: the first solver step pays PyTorch's one-time kernel setup for the
+    # loss's complex indexing and its backward (seconds on a fresh process)
+    adj.solve_gains(iq, win, data, model, ne, nch, ntaps, nsp, iters=2, tol=0.0, true_gains=g_true)
+    torch.cuda.synchronize()
     t0 = time.time()
     g, hist = adj.solve_gains(iq, win, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-11,
                               true_gains=g_true)

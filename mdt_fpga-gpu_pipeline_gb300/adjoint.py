@@ -108,11 +108,17 @@ def gain_error(est, true):
     """Relative error of estimated gains after removing each channel's global
     phase (which the baseline loss cannot see):  ||est e^{i phi} - true|| /
     ||true||, phi per channel from the best alignment; float."""
-    est = est.to(torch.complex128)
-    true = true.to(torch.complex128)
-    ph = (est.conj() * true).sum(dim=1, keepdim=True)
-    ph = ph / ph.abs().clamp_min(1e-300)
-    return float(torch.linalg.vector_norm(est * ph - true) / torch.linalg.vector_norm(true))
+    # plain real arithmetic (float64), so no complex128 reduction kernels are needed
+    e = torch.view_as_real(est.to(torch.complex64).contiguous()).double()
+    t = torch.view_as_real(true.to(torch.complex64).contiguous()).double()
+    er, ei, tr, ti = e[..., 0], e[..., 1], t[..., 0], t[..., 1]
+    pr = (er * tr + ei * ti).sum(dim=1, keepdim=True)   # sum conj(est) * true
+    pi = (er * ti - ei * tr).sum(dim=1, keepdim=True)
+    mag = torch.sqrt(pr * pr + pi * pi).clamp_min(1e-300)
+    cr, ci = pr / mag, pi / mag
+    dr = er * cr - ei * ci - tr
+    di = er * ci + ei * cr - ti
+    return float(torch.sqrt((dr * dr + di * di).sum() / (tr * tr + ti * ti).sum()))
 
 
 def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9, step=0.5,
@@ -131,7 +137,8 @@ def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9,
     Returns (gains complex64 [Nch, NE], history list of (loss, error or None))."""
     dev = iq.device
     mask = baseline_mask(ne, dev)
-    m2 = model.detach().to(torch.complex128).abs() ** 2  # [c, q, r]
+    mr = torch.view_as_real(model.detach().to(torch.complex64).contiguous()).double()
+    m2 = mr[..., 0] ** 2 + mr[..., 1] ** 2  # |model|^2, [c, q, r]
     m2 = m2 * (1 - torch.eye(ne, dtype=torch.float64, device=dev))
     g = torch.ones(nch, ne, dtype=torch.complex128, device=dev)
     data = data.detach()
