@@ -41,6 +41,8 @@ struct XengArgs {
     float2 alpha, beta;
     int beta_zero;
     int blocked;  // operand layout: 0 = X[k*ld + e]; 1 = XB[k/8][e][k%8] (NE rows per block)
+    int dual;     // NE <= 64: a block takes two channels (A and B buffers hold one each)
+    long nbatch;
 };
 
 __device__ __forceinline__ void pair_index(int p, int &I, int &J)
@@ -75,8 +77,11 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     auto tileA = [&](int st) { return sbuf + (size_t)(st * 2 + 0) * XS_KC * XS_RS; };
     auto tileB = [&](int st) { return sbuf + (size_t)(st * 2 + 1) * XS_KC * XS_RS; };
 
-    const int ch = blockIdx.x / a.npairs;
-    const int pr = blockIdx.x - ch * a.npairs;
+    // dual mode (single diagonal super-tile per channel): channels 2b and
+    // 2b+1, staged into the A and B buffers; otherwise one (channel, pair)
+    const int ch = a.dual ? 2 * (int)blockIdx.x : (int)blockIdx.x / a.npairs;
+    const int pr = a.dual ? 0 : (int)blockIdx.x - ch * a.npairs;
+    const bool has2 = a.dual && ch + 1 < a.nbatch;
     int I, J;
     pair_index(pr, I, J);
     const bool diag = (I == J);
@@ -84,10 +89,12 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     const int nr = min(XS_ST, a.ne - r0), nq = min(XS_ST, a.ne - q0);
     const int nmr = (nr + XS_MT - 1) / XS_MT, nmq = (nq + XS_MT - 1) / XS_MT;
     const int nmt = diag ? nmr * (nmr + 1) / 2 : nmr * nmq;
-    const int ksl = min(XS_KC, max(1, XS_THREADS / nmt));
+    const int nmt2 = a.dual ? 2 * nmt : nmt;  // micro-tiles of the block
+    const int ksl = min(XS_KC, max(1, XS_THREADS / nmt2));
     const int tid = threadIdx.x;
-    const bool active = tid < nmt * ksl;
-    const int mt = tid % nmt, ks = tid / nmt;
+    const int mt2 = tid % nmt2, ks = tid / nmt2;
+    const int cs = mt2 / nmt, mt = mt2 - cs * nmt;  // channel slot (dual), micro-tile
+    const bool active = tid < nmt2 * ksl && (cs == 0 || has2);
     int mi, mj;
     if (diag) {
         pair_index(mt, mi, mj);
@@ -97,6 +104,7 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     }
 
     const float2 *Xc = a.Xptrs ? a.Xptrs[ch] : a.X + (long)ch * a.xstride;
+    const float2 *Xc2 = !has2 ? Xc : (a.Xptrs ? a.Xptrs[ch + 1] : a.X + (long)(ch + 1) * a.xstride);
 
     // stage chunk k0 into buffer st: XS_KC x 64 complex per operand, [kk][e]
     auto stage = [&](int k0, int st) {
@@ -119,7 +127,10 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
             const bool ina = kin && e < nr;
             float2 *da = A + kk * XS_RS + e;
             cp_async8(da, ina ? Xc + off + (long)(r0 + e) * es : Xc, ina ? 8 : 0);
-            if (!diag) {
+            if (has2) {  // the second channel's rows go to the B buffer
+                cp_async8(B + kk * XS_RS + e, ina ? Xc2 + off + (long)(r0 + e) * es : Xc2,
+                          ina ? 8 : 0);
+            } else if (!diag) {
                 const bool inb = kin && e < nq;
                 cp_async8(B + kk * XS_RS + e, inb ? Xc + off + (long)(q0 + e) * es : Xc,
                           inb ? 8 : 0);
@@ -146,7 +157,7 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
         }
         __syncthreads();
         if (active) {
-            const float2 *A = tileA(st);
+            const float2 *A = cs ? tileB(st) : tileA(st);
             const float2 *B = diag ? A : tileB(st);
             for (int kk = ks; kk < XS_KC; kk += ksl) {
                 const float4 *pa = reinterpret_cast<const float4 *>(A + kk * XS_RS + mi * XS_MT);
@@ -178,7 +189,7 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
 #pragma unroll
             for (int i = 0; i < XS_MT; i++)
 #pragma unroll
-                for (int j = 0; j < XS_MT; j++) red[((ks - 1) * nmt + mt) * 16 + i * 4 + j] = acc[i][j];
+                for (int j = 0; j < XS_MT; j++) red[((ks - 1) * nmt2 + mt2) * 16 + i * 4 + j] = acc[i][j];
         }
         __syncthreads();
         if (active && ks == 0) {
@@ -187,7 +198,7 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
                 for (int i = 0; i < XS_MT; i++)
 #pragma unroll
                     for (int j = 0; j < XS_MT; j++) {
-                        float2 v = red[((s2 - 1) * nmt + mt) * 16 + i * 4 + j];
+                        float2 v = red[((s2 - 1) * nmt2 + mt2) * 16 + i * 4 + j];
                         acc[i][j].x += v.x;
                         acc[i][j].y += v.y;
                     }
@@ -196,7 +207,8 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     }
     if (!active || ks != 0) return;
 
-    float2 *Vc = a.Vptrs ? a.Vptrs[ch] : a.V + (long)ch * a.vstride;
+    const int cho = ch + cs;  // output channel
+    float2 *Vc = a.Vptrs ? a.Vptrs[cho] : a.V + (long)cho * a.vstride;
 #pragma unroll
     for (int i = 0; i < XS_MT; i++) {
 #pragma unroll
@@ -254,7 +266,13 @@ mdt_status xengine_herm_f32(int ne, long nbatch, int nsp, const float2 *X,
     a.beta = beta;
     a.beta_zero = beta_zero ? 1 : 0;
     a.blocked = blocked;
-    long blocks = nbatch * a.npairs;
+    a.nbatch = nbatch;
+    {
+        // two channels per block only while both channels' micro-tiles fit the block
+        const int nmr = (int)cdiv(ne, XS_MT);
+        a.dual = (a.nsuper == 1 && nmr * (nmr + 1) <= XS_THREADS) ? 1 : 0;
+    }
+    long blocks = a.dual ? (nbatch + 1) / 2 : nbatch * a.npairs;
     if (blocks > 0x7fffffffL) return invalid("xengine: grid too large");
     cudaError_t e = cudaFuncSetAttribute(xengine_herm_f32_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)XS_SMEM);

@@ -53,8 +53,11 @@ def test_fft_inverse_roundtrip_and_shim(mdt, cuda):
     assert mdt.cufftGetVersion() == 1000
 
 
+# (NE <= 60 runs two channels per block: odd channel counts leave a lone last channel;
+#  NE = 61..64 is a single diagonal super-tile that does not fit twice in a block)
 @pytest.mark.parametrize("ne,nch,nsp", [(3, 4, 2), (10, 8, 1000), (40, 6, 333), (64, 3, 64),
-                                        (65, 2, 100), (130, 2, 70), (256, 2, 96)])
+                                        (65, 2, 100), (130, 2, 70), (256, 2, 96), (60, 5, 40),
+                                        (61, 3, 40), (7, 1, 17)])
 def test_xengine_f32_vs_oracle(mdt, cuda, oracle, ne, nch, nsp):
     rng = np.random.default_rng(ne * 1000 + nsp)
     X = (rng.standard_normal((nch, nsp, ne)) + 1j * rng.standard_normal((nch, nsp, ne))
