@@ -59,7 +59,7 @@ extern "C" {
 typedef enum {
     MDT_SUCCESS = 0,
     MDT_ERR_INVALID_VALUE = 1, /* a size, pointer or parameter is out of range */
-    MDT_ERR_NOT_SUPPORTED = 2, /* valid request this build does not implement */
+    MDT_ERR_NOT_SUPPORTED = 2, /* valid request this library does not implement */
     MDT_ERR_CUDA = 3,          /* a CUDA runtime call failed; see mdt_last_error */
     MDT_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
     MDT_ERR_ALLOC = 5,         /* device or host allocation failed */
@@ -307,7 +307,7 @@ MDT_API mdt_status mdt_fx_get_timing(mdt_fx_plan plan, double *fengine_ms, doubl
                                      int *count);
 
 /* ------------------------------------------------------------------------
- * 4. Batches: many independent jobs of uneven shape (survey configuration
+ * 4. Batches: many independent jobs of uneven shape (benchmark configuration
  *    "24 ragged jobs"), f16 tensor-core path, Nch <= 2048, Ntaps 4 or 8.
  *    One F-engine launch per (Nch, Ntaps) group and one persistent X-engine
  *    launch over a work list spanning every job, captured in a CUDA graph on

@@ -232,7 +232,7 @@ MDT_API mdt_status mdt_fx_create(const mdt_fx_desc *desc, mdt_fx_plan *plan)
     if (st != MDT_SUCCESS) return st;
     if (desc->precision != MDT_PREC_FP32 && desc->precision != MDT_PREC_FP16 &&
         desc->precision != MDT_PREC_BF16 && desc->precision != MDT_PREC_INT8) {
-        mdt::set_error("fx_create: precision not supported by this build");
+        mdt::set_error("fx_create: precision not supported by this library");
         return MDT_ERR_NOT_SUPPORTED;
     }
     if (desc->precision != MDT_PREC_FP32 && desc->nchannels > 2048) {
