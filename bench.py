@@ -51,6 +51,31 @@ NCU_TRAFFIC_C3 = {"fengine_tc": 0.554507e9 * 8199 / 1031 + 1.032375e9 * 8,
                   "xengine_tc": 1.076980e9 * 8 + 0.484042e9}
 
 
+def bind_to_gpu_cpus(gpu_index):
+    """Restricts this process to the CPUs local to the GPU (sysfs local_cpulist
+    of its PCI device), so that pinned host buffers are allocated on the
+    GPU's NUMA node.  Returns the CPU list text, or None when unavailable."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=pci.bus_id",
+                              "--format=csv,noheader"], capture_output=True, text=True,
+                             timeout=30).stdout.strip().lower()
+        if not bus:
+            return None
+        dom, rest = bus.split(":", 1)
+        path = "/sys/bus/pci/devices/%s:%s/local_cpulist" % (dom[-4:], rest)
+        text = open(path).read().strip()
+        cpus = set()
+        for part in text.split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+            return text
+    except (OSError, ValueError, subprocess.SubprocessError):
+        return None
+    return None
+
+
 def load_pkg():
     return importlib.import_module("mdt_fpga-gpu_pipeline_gb300")
 
@@ -521,6 +546,8 @@ def run_ours(args, cfg):
     # ---- e2e through the host-buffer C-ABI entry (pinned host memory)
     e2e = None
     if not args.no_e2e:
+        all_cpus = os.sched_getaffinity(0)
+        host_cpus = bind_to_gpu_cpus(local)
         h_iq = torch.empty(total_sp * sb, dtype=torch.int8, pin_memory=True)
         h_iq.copy_(iq)
         h_vis = torch.empty(nint * nch * ne * ne * 2, dtype=torch.float32, pin_memory=True)
@@ -542,7 +569,9 @@ def run_ours(args, cfg):
         e2e = {"value": samples / e2e_s, "unit": "antenna-samples/s",
                "h2d_bytes_per_step": int(h_iq.numel()),
                "d2h_bytes_per_step": int(h_vis.numel() * 4),
-               "api": "mdt_fx_execute_host", "matches_device_run": bool(ok)}
+               "api": "mdt_fx_execute_host", "matches_device_run": bool(ok),
+               "host_cpus": host_cpus}
+        os.sched_setaffinity(0, all_cpus)  # the CPU baseline uses every core
 
     tensor = None
     if not args.no_tensor:
