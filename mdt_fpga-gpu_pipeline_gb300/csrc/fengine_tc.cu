@@ -18,11 +18,12 @@
 // (spectrum, k1), K is n2; B is the same real 64 x 64 form of the 32-point
 // DFT matrix for both.
 //
-// Work: one CTA per SM, two independent groups of 256 threads; a group walks
-// runs of up to 256 spectra of one element in units of 8 spectra (two
-// 128-row MMA tiles), carrying the last Ntaps-1 converted input rows in
-// registers, so every input sample is loaded (bulk copy of 2 KB rows into a
-// two-slot shared-memory ring) and converted once.
+// Work: one CTA per SM walks runs of up to 256 spectra of one element in
+// units of 8 spectra (two 128-row MMA tiles).  Warps 0-7 carry the last
+// Ntaps-1 converted input rows in registers, so every input sample is loaded
+// (bulk copy of 2 KB rows into a two-slot shared-memory ring) and converted
+// once; warps 8-15 run the twiddle and output stages of the previous unit
+// meanwhile (see fengine_tc_kernel).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -36,23 +37,27 @@ namespace mdt {
 namespace ftc {
 
 constexpr int N = 1024;
-constexpr int GROUPS = 2;
-constexpr int GTHREADS = 256;
-constexpr int THREADS = GROUPS * GTHREADS;
+constexpr int PT = 256;                 // PFB threads (warps 0-7)
+constexpr int ET = 256;                 // epilogue threads (warps 8-15)
+constexpr int THREADS = PT + ET;
 constexpr int US = 8;                   // spectra per unit
-constexpr int CPT = N / GTHREADS;       // channels per thread
+constexpr int CPT = N / PT;             // channels per PFB thread
 constexpr int ROWB = 2 * N;             // one (spectrum, element) row of int8 I/Q
 constexpr int RUN = 256;                // spectra per work item
 constexpr uint32_t TILE = 16384;        // 128 rows x 128 bytes
-// shared memory: DFT matrix, twiddles, int8 requantisation scales, then per
-// group: scaled window,
-// operand tiles (also the twiddled operand and the output staging), input ring
-constexpr uint32_t OFF_B = 0, OFF_TW = 8192, OFF_QS = 16384, OFF_G = 20480;
-constexpr uint32_t G_W = 0, G_A = 32768, G_RING = 65536, G_BYTES = 98304;
-constexpr uint32_t SMEM = OFF_G + GROUPS * G_BYTES;
-// TMEM: per group 256 columns -- two 64-column MMA tiles, then 64 columns
-// holding the packed output of the first 8 spectra of each 16-spectrum pair
-constexpr uint32_t TMEM_COLS = 512, TMEM_GROUP = 256, TMEM_STASH = 128;
+// shared memory: DFT matrix, twiddles, int8 requantisation scales, scaled
+// window, two P operand buffers (two tiles each), the Z operand, the output
+// staging S, the input ring (two slots of 8 rows)
+constexpr uint32_t OFF_B = 0, OFF_TW = 8192, OFF_QS = 16384, OFF_W = 20480;
+constexpr uint32_t OFF_P = 53248, OFF_Z = OFF_P + 4 * TILE, OFF_S = OFF_Z + 2 * TILE;
+constexpr uint32_t OFF_RING = OFF_S + 2 * TILE;
+constexpr uint32_t SMEM = OFF_RING + 2 * US * ROWB;
+// TMEM columns: MMA 1 accumulators (two buffers of two 64-column tiles), MMA 2
+// accumulators, then 64 columns holding the packed output of the first 8
+// spectra of each 16-spectrum pair
+constexpr uint32_t TMEM_COLS = 512, T_D1 = 0, T_D2 = 256, T_STASH = 384;
+// mbarriers
+enum { BAR_RING = 0, BAR_MMA1 = 2, BAR_FREE1 = 4, BAR_MMA2 = 6, NBARS = 7 };
 
 // One launch: a single job (with optional PFB history) or a device table of
 // jobs (FJob, work items from wk0).
@@ -195,17 +200,70 @@ __device__ __forceinline__ uint32_t tile_word(int r, int w)
     return (uint32_t)r * 128u + ((uint32_t)((w >> 2) ^ (r & 7)) << 4) + ((uint32_t)(w & 3) << 2);
 }
 
+// Bounded wait on an mbarrier phase that also gives up once the CTA's abort
+// flag is raised (so one role's failure does not leave the other spinning).
+__device__ __forceinline__ bool wait_or_abort(uint32_t bar, uint32_t parity, volatile int *abort)
+{
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (int k = 1; !tc::mbar_try_wait(bar, parity); k++) {
+        if ((k & 31) == 0 && *abort) return false;
+        if (clock64() - t0 > tc::kWaitCycles) return false;
+    }
+    return true;
+}
+
+// Work item w of the launch -> job (updates `a` / `cur`), element, first
+// spectrum, number of 8-spectrum units.
+struct Item {
+    int e, s0, nunits;
+};
+__device__ __forceinline__ bool next_job(const Launch &L, int w, FJob &a, int &cur)
+{
+    int j = cur < 0 ? 0 : cur;
+    if (L.table)
+        while (j + 1 < L.njobs && w >= L.table[j + 1].wk0) j++;
+    if (j == cur) return false;
+    if (L.table) a = L.table[j];
+    cur = j;
+    return true;
+}
+__device__ __forceinline__ Item item_of(const FJob &a, int w)
+{
+    const int runs_per_e = (a.nsp + RUN - 1) / RUN;
+    const int wl = w - a.wk0;
+    Item it;
+    it.e = wl / runs_per_e;
+    it.s0 = (wl % runs_per_e) * RUN;
+    it.nunits = (min(it.s0 + RUN, a.nsp) - it.s0 + US - 1) / US;
+    return it;
+}
+
+// One staged unit waiting for its copy-out.
+struct OutUnit {
+    uint8_t *X16;
+    int nep, e, kc, j0, nvalid;
+    bool second, lone;
+};
+
+// Warp-specialised pipeline, one CTA per SM.  Warps 0-7 (PFB role) stream
+// the input, run the tap sum into P buffer u % 2 and issue MMA 1 into TMEM
+// D1 buffer u % 2.  Warps 8-15 (epilogue role) read D1, apply the twiddles
+// into Z, issue MMA 2, store the previous unit (from the staging buffer S)
+// while MMA 2 works, then pack this unit's result into S.  The roles meet
+// only at mbarriers: MMA 1 done (P and D1 written / read) and D1 free
+// (epilogue has read D1), so the PFB of unit u + 1 runs while the epilogue
+// of unit u works.
 template <int NT, int MODE>
 __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
 {
     extern __shared__ __align__(1024) uint8_t sm[];
-    __shared__ uint64_t bars[GROUPS][3];  // ring slot 0, ring slot 1, MMA done
+    __shared__ uint64_t bars[NBARS];
     __shared__ uint32_t tmem_slot;
-    __shared__ int abort_flag[GROUPS];
+    __shared__ int abort_flag;
 
     const uint32_t sbase = tc::smem_u32(sm);
     const int tid = threadIdx.x;
-    const int g = tid / GTHREADS, t = tid % GTHREADS, wg = t >> 5, l = t & 31;
 
     if (sbase & 1023) {  // the operand tiles need 1024-byte alignment
         if (tid == 0) atomicExch(L.err, 2);
@@ -235,9 +293,9 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     if constexpr (MODE == OUT_Q8)
         for (int i = tid; i < N; i += THREADS) qs_s[i] = __ldg(L.qscales + i);
     if (tid == 0) {
-        for (int gg = 0; gg < GROUPS; gg++)
-            for (int b = 0; b < 3; b++) tc::mbar_init(tc::smem_u32(&bars[gg][b]), 1);
-        abort_flag[0] = abort_flag[1] = 0;
+        for (int b = 0; b < NBARS; b++)
+            tc::mbar_init(tc::smem_u32(&bars[b]), (b == BAR_FREE1 || b == BAR_FREE1 + 1) ? ET : 1);
+        abort_flag = 0;
         tc::fence_mbar_init();
     }
     if (tid < 32) {
@@ -248,302 +306,348 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     tc::fence_proxy_async();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = tmem_slot + (uint32_t)(g * TMEM_GROUP);
-    const uint32_t lane_q = (uint32_t)((wg & 3) * 32) << 16;
-
-    // ---------------------------------------------------------------- group
-    const uint32_t gA = sbase + OFF_G + (uint32_t)g * G_BYTES + G_A;     // tiles / A' / staging
-    const uint32_t gR = sbase + OFF_G + (uint32_t)g * G_BYTES + G_RING;  // input ring, 2 x 8 rows
-    // scaled window, tap pairs: wsp[p][wpos(c)] = (W[2p][c], W[2p+1][c]) * scale
-    float2 *wsp = reinterpret_cast<float2 *>(sm + OFF_G + (size_t)g * G_BYTES + G_W);
-    const uint32_t wsp_s = sbase + OFF_G + (uint32_t)g * G_BYTES + G_W;
-    const uint32_t bar_in0 = tc::smem_u32(&bars[g][0]), bar_in1 = tc::smem_u32(&bars[g][1]);
-    const uint32_t bar_mma = tc::smem_u32(&bars[g][2]);
-    uint32_t ph_in0 = 0, ph_in1 = 0, ph_mma = 0;
-    bool pend0 = false, pend1 = false;  // loads in flight (for the drain on abort)
-    const bool issuer = (t == 0);
-    const int bar_id = 1 + g;
-
-    int cn1[CPT], cn2[CPT];
-#pragma unroll
-    for (int j = 0; j < CPT; j++) chan_of(8 * j + wg, l, cn1[j], cn2[j]);
-
-    const uint32_t id_mma = tc::idesc_f16(64, 0, 0);  // M 128, N 64, f16 operands
-    const uint64_t bdesc = tc::sw128_kmajor_desc(sbase + OFF_B);
-    uint64_t carry[CPT][NT - 1];
-    bool ok = true;
-
-    FJob a = L.one;   // the current job
-    int cur = -1;     // its index (-1: none loaded)
-    const int nhist = L.table ? 0 : L.nhist;
-    auto row_src = [&](long rho, int e) -> const char2 * {
-        return rho < nhist ? L.hist + (rho * a.ne + e) * (long)N
-                           : a.iq + ((rho - nhist) * a.ne + e) * (long)N;
-    };
-    // issue the bulk copies of rows [r0, r0 + cnt) of element e into slot s
-    auto load_rows = [&](int s, long r0, int cnt, int e) {
-        const uint32_t bar = s ? bar_in1 : bar_in0;
-        tc::mbar_expect_tx(bar, (uint32_t)(cnt * ROWB));
-        for (int r = 0; r < cnt; r++)
-            tc::bulk_g2s(gR + (uint32_t)(s * 8 * ROWB + r * ROWB), row_src(r0 + r, e), ROWB, bar);
-    };
-    auto sync_group = [&]() { tc::named_barrier(bar_id, GTHREADS); };
+    const uint32_t tmem = tmem_slot;
+    volatile int *abortp = &abort_flag;
+    // A failed wait raises the CTA's abort flag (which ends the other role's
+    // waits early) and the thread's own flag; each role leaves its loop only
+    // at a barrier that ORs the threads' flags, so all its threads leave
+    // together and none is left at a named barrier.
+    bool bad = false;
     auto fail = [&]() {
         atomicExch(L.err, 1);
-        abort_flag[g] = 1;
+        *abortp = 1;
+        bad = true;
     };
+    const uint32_t id_mma = tc::idesc_f16(64, 0, 0);  // M 128, N 64, f16 operands
+    const uint64_t bdesc = tc::sw128_kmajor_desc(sbase + OFF_B);
+    const uint32_t bar_mma1 = tc::smem_u32(&bars[BAR_MMA1]);    // + 8 * b
+    const uint32_t bar_free1 = tc::smem_u32(&bars[BAR_FREE1]);  // + 8 * b
+    const uint32_t bar_mma2 = tc::smem_u32(&bars[BAR_MMA2]);
+    const uint32_t gZ = sbase + OFF_Z;
 
-    for (int w = blockIdx.x * GROUPS + g; w < L.nwork && ok; w += gridDim.x * GROUPS) {
-        // the job of work item w (items are ascending, so the job index only grows)
-        int j = cur < 0 ? 0 : cur;
-        if (L.table)
-            while (j + 1 < L.njobs && w >= L.table[j + 1].wk0) j++;
-        if (j != cur) {
-            if (L.table) a = L.table[j];
-            cur = j;
-            sync_group();  // the previous job's window is no longer read
-            for (int i = t; i < N * 4; i += GTHREADS) {
-                const int pr = i >> 10, c = i & (N - 1);
-                const float w0 = 2 * pr < NT ? __ldg(a.win + 2 * pr * N + c) * a.scale : 0.0f;
-                const float w1 = 2 * pr + 1 < NT ? __ldg(a.win + (2 * pr + 1) * N + c) * a.scale : 0.0f;
-                wsp[pr * N + wpos(c)] = make_float2(w0, w1);
-            }
-            sync_group();
-        }
-        const int runs_per_e = (a.nsp + RUN - 1) / RUN;
-        const int wl = w - a.wk0;
-        const int e = wl / runs_per_e;
-        const int s0 = (wl % runs_per_e) * RUN;
-        const int s1 = min(s0 + RUN, a.nsp);
-        const int nunits = (s1 - s0 + US - 1) / US;
-        auto unit_rows = [&](int u) {
-            const int r = a.nsp - s0 - US * u;
-            return r < 0 ? 0 : (r > US ? US : r);
+    if (tid < PT) {
+        // ============================================================ PFB role
+        const int t = tid, wg = t >> 5, l = t & 31;
+        const uint32_t gR = sbase + OFF_RING;
+        // scaled window, tap pairs: wsp[p][wpos(c)] = (W[2p][c], W[2p+1][c]) * scale
+        float2 *wsp = reinterpret_cast<float2 *>(sm + OFF_W);
+        const uint32_t wsp_s = sbase + OFF_W;
+        const uint32_t bar_in0 = tc::smem_u32(&bars[BAR_RING]), bar_in1 = bar_in0 + 8;
+        uint32_t ph_in0 = 0, ph_in1 = 0;
+        bool pend0 = false, pend1 = false;  // loads in flight (for the drain on abort)
+        const bool issuer = (t == 0);
+        long last_mma = -1;
+        int cn1[CPT], cn2[CPT];
+#pragma unroll
+        for (int j = 0; j < CPT; j++) chan_of(8 * j + wg, l, cn1[j], cn2[j]);
+        uint64_t carry[CPT][NT - 1];
+        bool ok = true;
+        long n = 0;  // units of this CTA so far
+        FJob a = L.one;
+        int cur = -1;
+        const int nhist = L.table ? 0 : L.nhist;
+        auto row_src = [&](long rho, int e) -> const char2 * {
+            return rho < nhist ? L.hist + (rho * a.ne + e) * (long)N
+                               : a.iq + ((rho - nhist) * a.ne + e) * (long)N;
         };
-        // lead-in rows into slot 1, unit 0 into slot 0
-        if (issuer) {
-            load_rows(1, s0, NT - 1, e);
-            load_rows(0, s0 + NT - 1, unit_rows(0), e);
-        }
-        pend0 = pend1 = true;
-        if (!tc::mbar_wait(bar_in1, ph_in1)) fail();
-        ph_in1 ^= 1;
-        pend1 = false;
-#pragma unroll
-        for (int j = 0; j < CPT; j++) {
-            const uint32_t cb = (uint32_t)(2 * (32 * cn1[j] + cn2[j]));
-#pragma unroll
-            for (int i = 0; i < NT - 1; i++)
-                carry[j][i] = iq_to_f2(lds_u16(gR + (uint32_t)(8 * ROWB + i * ROWB) + cb));
-        }
-        sync_group();
-        if (abort_flag[g]) {
-            ok = false;
-            break;
-        }
-        if (issuer && nunits > 1) load_rows(1, s0 + US + NT - 1, unit_rows(1), e);
-        pend1 = nunits > 1;
+        // issue the bulk copies of rows [r0, r0 + cnt) of element e into slot s
+        auto load_rows = [&](int s, long r0, int cnt, int e) {
+            const uint32_t bar = s ? bar_in1 : bar_in0;
+            tc::mbar_expect_tx(bar, (uint32_t)(cnt * ROWB));
+            for (int r = 0; r < cnt; r++)
+                tc::bulk_g2s(gR + (uint32_t)(s * 8 * ROWB + r * ROWB), row_src(r0 + r, e), ROWB, bar);
+        };
+        auto sync_pfb = [&]() { tc::named_barrier(1, PT); };
+        auto sync_pfb_bad = [&]() { return tc::named_barrier_or(1, PT, bad); };
 
-        for (int u = 0; u < nunits; u++) {
-            const int slot = u & 1;
-            const uint32_t ring = gR + (uint32_t)(slot * 8 * ROWB);
-            if (!tc::mbar_wait(slot ? bar_in1 : bar_in0, slot ? ph_in1 : ph_in0)) fail();
-            if (slot) {
-                ph_in1 ^= 1;
-                pend1 = false;
-            } else {
-                ph_in0 ^= 1;
-                pend0 = false;
+        for (int w = blockIdx.x; w < L.nwork && ok; w += gridDim.x) {
+            if (next_job(L, w, a, cur)) {
+                sync_pfb();  // the previous job's window is no longer read
+                for (int i = t; i < N * 4; i += PT) {
+                    const int pr = i >> 10, c = i & (N - 1);
+                    const float w0 = 2 * pr < NT ? __ldg(a.win + 2 * pr * N + c) * a.scale : 0.0f;
+                    const float w1 =
+                        2 * pr + 1 < NT ? __ldg(a.win + (2 * pr + 1) * N + c) * a.scale : 0.0f;
+                    wsp[pr * N + wpos(c)] = make_float2(w0, w1);
+                }
+                sync_pfb();
             }
-            // ---- PFB: 8 spectra x 4 channels per thread -> A tiles (f16, scaled)
+            const Item it = item_of(a, w);
+            const int e = it.e, s0 = it.s0, nunits = it.nunits;
+            auto unit_rows = [&](int u) {
+                const int r = a.nsp - s0 - US * u;
+                return r < 0 ? 0 : (r > US ? US : r);
+            };
+            // lead-in rows into slot 1, unit 0 into slot 0
+            if (issuer) {
+                load_rows(1, s0, NT - 1, e);
+                load_rows(0, s0 + NT - 1, unit_rows(0), e);
+            }
+            pend0 = pend1 = true;
+            if (!wait_or_abort(bar_in1, ph_in1, abortp)) fail();
+            ph_in1 ^= 1;
+            pend1 = false;
 #pragma unroll
             for (int j = 0; j < CPT; j++) {
-                const int n1 = cn1[j], n2 = cn2[j];
-                const int c = 32 * n1 + n2;
-                uint64_t w2[NT];
+                const uint32_t cb = (uint32_t)(2 * (32 * cn1[j] + cn2[j]));
 #pragma unroll
-                for (int pr = 0; pr < NT / 2; pr++) {
-                    const float2 wv = lds_f2(wsp_s + (uint32_t)((pr * N + wpos(c)) * 8));
-                    w2[2 * pr] = pk2(wv.x, wv.x);
-                    w2[2 * pr + 1] = pk2(wv.y, wv.y);
-                }
-                uint64_t xw[NT - 1 + US];
-#pragma unroll
-                for (int i = 0; i < NT - 1; i++) xw[i] = carry[j][i];
-#pragma unroll
-                for (int r = 0; r < US; r++)
-                    xw[NT - 1 + r] = iq_to_f2(lds_u16(ring + (uint32_t)(r * ROWB + 2 * c)));
-#pragma unroll
-                for (int s = 0; s < US; s++) {
-                    uint64_t acc = mul2(xw[s], w2[0]);
-#pragma unroll
-                    for (int i = 1; i < NT; i++) acc = fma2(xw[s + i], w2[i], acc);
-                    const float2 p = up2(acc);
-                    const int row = (s & 3) * 32 + n2;
-                    sts_u32(gA + (uint32_t)(s >> 2) * TILE + tile_word(row, n1),
-                            pack_h2<__half>(p.x, p.y));
-                }
-#pragma unroll
-                for (int i = 0; i < NT - 1; i++) carry[j][i] = xw[US + i];
+                for (int i = 0; i < NT - 1; i++)
+                    carry[j][i] = iq_to_f2(lds_u16(gR + (uint32_t)(8 * ROWB + i * ROWB) + cb));
             }
-            tc::fence_proxy_async();
-            sync_group();
-            if (abort_flag[g]) {
+            if (sync_pfb_bad()) {
                 ok = false;
                 break;
             }
-            if (issuer) {
+            if (issuer && nunits > 1) load_rows(1, s0 + US + NT - 1, unit_rows(1), e);
+            pend1 = nunits > 1;
+
+            for (int u = 0; u < nunits; u++, n++) {
+                const int slot = u & 1, b = (int)(n & 1);
+                const uint32_t ring = gR + (uint32_t)(slot * 8 * ROWB);
+                if (!wait_or_abort(slot ? bar_in1 : bar_in0, slot ? ph_in1 : ph_in0, abortp)) fail();
+                if (slot) {
+                    ph_in1 ^= 1;
+                    pend1 = false;
+                } else {
+                    ph_in0 ^= 1;
+                    pend0 = false;
+                }
+                // P buffer b is free once MMA 1 of unit n - 2 has completed
+                if (n >= 2 && !wait_or_abort(bar_mma1 + 8 * b, (uint32_t)(((n >> 1) & 1) ^ 1), abortp))
+                    fail();
+                const uint32_t gP = sbase + OFF_P + (uint32_t)b * 2 * TILE;
+                // ---- PFB: 8 spectra x 4 channels per thread -> P tiles (f16, scaled)
+#pragma unroll
+                for (int j = 0; j < CPT; j++) {
+                    const int n1 = cn1[j], n2 = cn2[j];
+                    const int c = 32 * n1 + n2;
+                    uint64_t w2[NT];
+#pragma unroll
+                    for (int pr = 0; pr < NT / 2; pr++) {
+                        const float2 wv = lds_f2(wsp_s + (uint32_t)((pr * N + wpos(c)) * 8));
+                        w2[2 * pr] = pk2(wv.x, wv.x);
+                        w2[2 * pr + 1] = pk2(wv.y, wv.y);
+                    }
+                    uint64_t xw[NT - 1 + US];
+#pragma unroll
+                    for (int i = 0; i < NT - 1; i++) xw[i] = carry[j][i];
+#pragma unroll
+                    for (int r = 0; r < US; r++)
+                        xw[NT - 1 + r] = iq_to_f2(lds_u16(ring + (uint32_t)(r * ROWB + 2 * c)));
+#pragma unroll
+                    for (int s = 0; s < US; s++) {
+                        uint64_t acc = mul2(xw[s], w2[0]);
+#pragma unroll
+                        for (int i = 1; i < NT; i++) acc = fma2(xw[s + i], w2[i], acc);
+                        const float2 p = up2(acc);
+                        const int row = (s & 3) * 32 + n2;
+                        sts_u32(gP + (uint32_t)(s >> 2) * TILE + tile_word(row, n1),
+                                pack_h2<__half>(p.x, p.y));
+                    }
+#pragma unroll
+                    for (int i = 0; i < NT - 1; i++) carry[j][i] = xw[US + i];
+                }
+                tc::fence_proxy_async();
+                if (sync_pfb_bad()) {
+                    ok = false;
+                    break;
+                }
+                if (issuer) {
+                    if (u + 2 < nunits) load_rows(slot, s0 + US * (u + 2) + NT - 1, unit_rows(u + 2), e);
+                    // D1 buffer b is free once the epilogue has read unit n - 2
+                    if (n >= 2 && !wait_or_abort(bar_free1 + 8 * b, (uint32_t)(((n >> 1) & 1) ^ 1), abortp)) {
+                        fail();
+                    } else {
+                        tc::fence_after_sync();
+#pragma unroll
+                        for (int tl = 0; tl < 2; tl++) {
+                            const uint64_t ad = tc::sw128_kmajor_desc(gP + (uint32_t)tl * TILE);
+#pragma unroll
+                            for (int k = 0; k < 4; k++)
+                                tc::mma_f16(tmem + T_D1 + (uint32_t)(b * 128 + tl * 64), ad + 2 * k,
+                                            bdesc + 2 * k, id_mma, k > 0);
+                        }
+                        tc::mma_commit(bar_mma1 + 8 * b);
+                        last_mma = n;
+                    }
+                }
                 if (u + 2 < nunits) {
-                    load_rows(slot, s0 + US * (u + 2) + NT - 1, unit_rows(u + 2), e);
+                    if (slot) pend1 = true;
+                    else pend0 = true;
                 }
+            }
+        }
+        // drain what is still in flight, bounded (copies only after an abort)
+        if (issuer) {
+            if (!ok) {
+                if (pend0) tc::mbar_wait(bar_in0, ph_in0);
+                if (pend1) tc::mbar_wait(bar_in1, ph_in1);
+            }
+            if (last_mma >= 0)
+                tc::mbar_wait(bar_mma1 + 8 * (uint32_t)(last_mma & 1), (uint32_t)((last_mma >> 1) & 1));
+        }
+    } else {
+        // ======================================================= epilogue role
+        const int t = tid - PT, wg = t >> 5, l = t & 31;
+        const uint32_t lane_q = (uint32_t)((wg & 3) * 32) << 16;  // warp (8 + wg) reads lanes 32 (wg % 4) ..
+        const int tl = wg >> 2, qd = wg & 3;
+        const int su = tl * 4 + qd;  // spectrum of this thread's D1 / D2 rows within the unit
+        const bool issuer = (t == 0);
+        const uint32_t gS = sbase + OFF_S;
+        const uint32_t stash = tmem + lane_q + T_STASH + (uint32_t)(tl * 32);
+        long last_mma = -1;
+        bool ok = true;
+        long n = 0;
+        FJob a = L.one;
+        int cur = -1;
+        auto sync_epi = [&]() { tc::named_barrier(2, ET); };
+        auto sync_epi_bad = [&]() { return tc::named_barrier_or(2, ET, bad); };
+
+        // Copy-out of a staged unit.  Units pair up into 16 spectra: the first
+        // unit's packed 16-byte re and im chunks wait in TMEM, the second writes
+        // both units' chunks as full 32-byte sectors (re chunks j, j+1 and im
+        // chunks 4+j, 5+j of a row are sector neighbours under the row swizzle).
+        OutUnit prev{};
+        bool have_prev = false;
+        auto copy_out = [&](const OutUnit &o) {
+            uint32_t p0[16];  // the first unit's words of two channels (second unit only)
+            const bool stash_only = !o.second && !o.lone;
+            const bool swap = (o.e & 1) != 0;  // the odd chunk comes first in the sector
+            const uint32_t sre = (uint32_t)(((o.j0 ^ (o.e & 7)) & ~1) << 4);
+            const uint32_t sim = (uint32_t)((((4 + o.j0) ^ (o.e & 7)) & ~1) << 4);
+#pragma unroll
+            for (int j = 0; j < CPT; j++) {
+                const int c = t + ET * j;
+                if (o.second && (j & 1) == 0) {  // stash reads of channels j, j + 1
+                    tc::tmem_ld8(stash + (uint32_t)(8 * j), *reinterpret_cast<uint32_t(*)[8]>(p0));
+                    tc::tmem_ld8(stash + (uint32_t)(8 * j + 8), *reinterpret_cast<uint32_t(*)[8]>(p0 + 8));
+                }
+                uint32_t wv[US];
+#pragma unroll
+                for (int s = 0; s < US; s++)
+                    wv[s] = lds_u32(gS + (uint32_t)(c * 32) + (uint32_t)((s ^ ((c >> 2) & 7)) << 2));
+                if (o.nvalid < US) {
+#pragma unroll
+                    for (int s = 0; s < US; s++)
+                        if (s >= o.nvalid) wv[s] = 0u;
+                }
+                uint32_t pk[8];  // re (4 words: 8 spectra) then im
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    pk[q] = __byte_perm(wv[2 * q], wv[2 * q + 1], 0x5410);
+                    pk[4 + q] = __byte_perm(wv[2 * q], wv[2 * q + 1], 0x7632);
+                }
+                if (stash_only) {
+                    tc::tmem_st8(stash + (uint32_t)(8 * j), pk);
+                    continue;
+                }
+                if (o.second && (j & 1) == 0) tc::tmem_ld_wait();
+                const uint32_t *fw = o.second ? p0 + 8 * (j & 1) : pk;  // first unit's words
+                const uint4 fr = make_uint4(fw[0], fw[1], fw[2], fw[3]);
+                const uint4 fi = make_uint4(fw[4], fw[5], fw[6], fw[7]);
+                const uint4 sr = o.second ? make_uint4(pk[0], pk[1], pk[2], pk[3]) : make_uint4(0u, 0u, 0u, 0u);
+                const uint4 si = o.second ? make_uint4(pk[4], pk[5], pk[6], pk[7]) : make_uint4(0u, 0u, 0u, 0u);
+                uint8_t *row = o.X16 + (((size_t)o.kc * N + c) * o.nep + o.e) * 128;
+                if (swap) {
+                    stg32(row + sre, sr, fr);
+                    stg32(row + sim, si, fi);
+                } else {
+                    stg32(row + sre, fr, sr);
+                    stg32(row + sim, fi, si);
+                }
+            }
+            if (stash_only) tc::tmem_st_wait();
+        };
+
+        for (int w = blockIdx.x; w < L.nwork && ok; w += gridDim.x) {
+            next_job(L, w, a, cur);
+            const Item it = item_of(a, w);
+            const int e = it.e, s0 = it.s0, nunits = it.nunits;
+            for (int u = 0; u < nunits; u++, n++) {
+                const int b = (int)(n & 1);
+                // ---- twiddle: D1 (row = (spectrum, n2), col = k1) -> Z (row = (spectrum, k1), K = n2)
+                if (!wait_or_abort(bar_mma1 + 8 * b, (uint32_t)((n >> 1) & 1), abortp)) fail();
                 tc::fence_after_sync();
+                {
+                    const uint32_t tbase = tmem + lane_q + T_D1 + (uint32_t)(b * 128 + tl * 64);
+                    uint32_t v[64];
 #pragma unroll
-                for (int tl = 0; tl < 2; tl++) {
-                    const uint64_t ad = tc::sw128_kmajor_desc(gA + (uint32_t)tl * TILE);
-#pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        tc::mma_f16(tmem + (uint32_t)(tl * 64), ad + 2 * k, bdesc + 2 * k, id_mma,
-                                    k > 0);
-                }
-                tc::mma_commit(bar_mma);
-            }
-            if (u + 2 < nunits) {
-                if (slot) pend1 = true;
-                else pend0 = true;
-            }
-            // ---- twiddle: TMEM (row = (spectrum, n2), col = k1) -> A' (row = (spectrum, k1), K = n2)
-            if (!tc::mbar_wait(bar_mma, ph_mma)) fail();
-            ph_mma ^= 1;
-            tc::fence_after_sync();
-            {
-                const int tl = wg >> 2, qd = wg & 3;
-                const uint32_t tbase = tmem + lane_q + (uint32_t)(tl * 64);
-                const uint32_t abase = gA + (uint32_t)tl * TILE;
-#pragma unroll
-                for (int half = 0; half < 2; half++) {
-                    uint32_t v[32];
-                    tc::tmem_ld16(tbase + (uint32_t)(half * 32), *reinterpret_cast<uint32_t(*)[16]>(v));
-                    tc::tmem_ld16(tbase + (uint32_t)(half * 32 + 16),
-                                  *reinterpret_cast<uint32_t(*)[16]>(v + 16));
+                    for (int q = 0; q < 4; q++)
+                        tc::tmem_ld16(tbase + (uint32_t)(16 * q), *reinterpret_cast<uint32_t(*)[16]>(v + 16 * q));
                     tc::tmem_ld_wait();
+                    tc::fence_before_sync();
+                    tc::mbar_arrive(bar_free1 + 8 * b);
+                    const uint32_t abase = gZ + (uint32_t)tl * TILE;
 #pragma unroll
-                    for (int kk = 0; kk < 16; kk++) {
-                        const int k1 = half * 16 + kk;
-                        const float yr = __uint_as_float(v[2 * kk]), yi = __uint_as_float(v[2 * kk + 1]);
-                        const float2 w = tw[k1 * 32 + l];
-                        const float zr = fmaf(yr, w.x, -yi * w.y);
-                        const float zi = fmaf(yr, w.y, yi * w.x);
+                    for (int k1 = 0; k1 < 32; k1++) {
+                        const float yr = __uint_as_float(v[2 * k1]), yi = __uint_as_float(v[2 * k1 + 1]);
+                        const float2 tv = tw[k1 * 32 + l];
+                        const float zr = fmaf(yr, tv.x, -yi * tv.y);
+                        const float zi = fmaf(yr, tv.y, yi * tv.x);
                         sts_u32(abase + tile_word(qd * 32 + k1, l), pack_h2<__half>(zr, zi));
                     }
                 }
-            }
-            tc::fence_proxy_async();
-            tc::fence_before_sync();
-            sync_group();
-            if (issuer) {
+                tc::fence_proxy_async();
+                if (sync_epi_bad()) {  // also orders the previous unit's staging before its copy-out
+                    ok = false;
+                    break;
+                }
+                if (issuer) {
+                    tc::fence_after_sync();
+#pragma unroll
+                    for (int tt = 0; tt < 2; tt++) {
+                        const uint64_t ad = tc::sw128_kmajor_desc(gZ + (uint32_t)tt * TILE);
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            tc::mma_f16(tmem + T_D2 + (uint32_t)(tt * 64), ad + 2 * k, bdesc + 2 * k,
+                                        id_mma, k > 0);
+                    }
+                    tc::mma_commit(bar_mma2);
+                    last_mma = n;
+                }
+                // ---- the previous unit's copy-out runs while MMA 2 works
+                if (have_prev) copy_out(prev);
+                // ---- output: D2 (row = (spectrum, k1), col = k2) -> staging S [channel][spectrum]
+                if (!wait_or_abort(bar_mma2, (uint32_t)(n & 1), abortp)) fail();
                 tc::fence_after_sync();
+                uint32_t v[64];
+                {
+                    const uint32_t tbase = tmem + lane_q + T_D2 + (uint32_t)(tl * 64);
 #pragma unroll
-                for (int tl = 0; tl < 2; tl++) {
-                    const uint64_t ad = tc::sw128_kmajor_desc(gA + (uint32_t)tl * TILE);
-#pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        tc::mma_f16(tmem + (uint32_t)(tl * 64), ad + 2 * k, bdesc + 2 * k, id_mma,
-                                    k > 0);
-                }
-                tc::mma_commit(bar_mma);
-            }
-            // ---- output: TMEM (row = (spectrum, k1), col = k2) -> staging [channel][spectrum]
-            if (!tc::mbar_wait(bar_mma, ph_mma)) fail();
-            ph_mma ^= 1;
-            tc::fence_after_sync();
-            {
-                const int tl = wg >> 2, qd = wg & 3;
-                const int su = tl * 4 + qd;  // spectrum within the unit
-                const uint32_t tbase = tmem + lane_q + (uint32_t)(tl * 64);
-#pragma unroll
-                for (int half = 0; half < 2; half++) {
-                    uint32_t v[32];
-                    tc::tmem_ld16(tbase + (uint32_t)(half * 32), *reinterpret_cast<uint32_t(*)[16]>(v));
-                    tc::tmem_ld16(tbase + (uint32_t)(half * 32 + 16),
-                                  *reinterpret_cast<uint32_t(*)[16]>(v + 16));
+                    for (int q = 0; q < 4; q++)
+                        tc::tmem_ld16(tbase + (uint32_t)(16 * q), *reinterpret_cast<uint32_t(*)[16]>(v + 16 * q));
                     tc::tmem_ld_wait();
+                }
+                tc::fence_before_sync();
+                sync_epi();  // S is no longer read by the previous copy-out
 #pragma unroll
-                    for (int kk = 0; kk < 16; kk++) {
-                        const int c = l + 32 * (half * 16 + kk);
-                        const float qs = MODE == OUT_Q8 ? qs_s[c] : 1.0f;
-                        sts_u32(gA + (uint32_t)(c * 32) + (uint32_t)((su ^ ((c >> 2) & 7)) << 2),
-                                pack_out<MODE>(__uint_as_float(v[2 * kk]),
-                                               __uint_as_float(v[2 * kk + 1]), qs));
-                    }
+                for (int kk = 0; kk < 32; kk++) {
+                    const int c = l + 32 * kk;
+                    const float qs = MODE == OUT_Q8 ? qs_s[c] : 1.0f;
+                    sts_u32(gS + (uint32_t)(c * 32) + (uint32_t)((su ^ ((c >> 2) & 7)) << 2),
+                            pack_out<MODE>(__uint_as_float(v[2 * kk]), __uint_as_float(v[2 * kk + 1]), qs));
+                }
+                {
+                    const int sabs = s0 + US * u;
+                    const bool second = (u & 1) != 0;
+                    const int s_first = second ? sabs - US : sabs;
+                    prev.X16 = a.X16;
+                    prev.nep = a.nep;
+                    prev.e = e;
+                    prev.kc = s_first >> 5;
+                    prev.j0 = (s_first & 31) >> 3;  // even
+                    prev.nvalid = min(US, a.nsp - sabs);
+                    prev.second = second;
+                    prev.lone = !second && u + 1 == nunits;  // first unit without a partner
+                    have_prev = true;
                 }
             }
-            tc::fence_before_sync();
-            sync_group();
-            // ---- copy-out.  Units pair up into 16 spectra: the first unit's packed
-            // 16-byte re and im chunks wait in TMEM, the second writes both units'
-            // chunks as full 32-byte sectors (re chunks j, j+1 and im chunks 4+j,
-            // 5+j of a row are sector neighbours under the row swizzle).
-            {
-                const int sabs = s0 + US * u;
-                const int nvalid = min(US, a.nsp - sabs);
-                const bool second = (u & 1) != 0;
-                const bool lone = !second && u + 1 == nunits;  // first unit without a partner
-                const uint32_t stash = tmem + lane_q + TMEM_STASH + (uint32_t)((wg >> 2) * 32);
-                const int s_first = second ? sabs - US : sabs;
-                const int kc = s_first >> 5, j0 = (s_first & 31) >> 3;  // j0 even
-                const bool swap = (e & 1) != 0;  // the odd chunk comes first in the sector
-                const uint32_t sre = (uint32_t)(((j0 ^ (e & 7)) & ~1) << 4);
-                const uint32_t sim = (uint32_t)((((4 + j0) ^ (e & 7)) & ~1) << 4);
-#pragma unroll
-                for (int j = 0; j < CPT; j++) {
-                    const int c = t + GTHREADS * j;
-                    uint32_t wv[US];
-#pragma unroll
-                    for (int s = 0; s < US; s++) {
-                        const uint32_t x = lds_u32(gA + (uint32_t)(c * 32) +
-                                                   (uint32_t)((s ^ ((c >> 2) & 7)) << 2));
-                        wv[s] = s < nvalid ? x : 0u;
-                    }
-                    uint32_t pk[8];  // re (4 words: 8 spectra) then im
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        pk[q] = __byte_perm(wv[2 * q], wv[2 * q + 1], 0x5410);
-                        pk[4 + q] = __byte_perm(wv[2 * q], wv[2 * q + 1], 0x7632);
-                    }
-                    if (!second && !lone) {
-                        tc::tmem_st8(stash + (uint32_t)(8 * j), pk);
-                        continue;
-                    }
-                    uint32_t p0[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};  // first unit (zero if lone)
-                    if (second) {
-                        tc::tmem_ld8(stash + (uint32_t)(8 * j), p0);
-                        tc::tmem_ld_wait();
-                    }
-                    const uint32_t *fw = second ? p0 : pk;  // first unit's words
-                    const uint4 fr = make_uint4(fw[0], fw[1], fw[2], fw[3]);
-                    const uint4 fi = make_uint4(fw[4], fw[5], fw[6], fw[7]);
-                    const uint4 sr = second ? make_uint4(pk[0], pk[1], pk[2], pk[3])
-                                            : make_uint4(0u, 0u, 0u, 0u);
-                    const uint4 si = second ? make_uint4(pk[4], pk[5], pk[6], pk[7])
-                                            : make_uint4(0u, 0u, 0u, 0u);
-                    uint8_t *row = a.X16 + (((size_t)kc * N + c) * a.nep + e) * 128;
-                    if (swap) {
-                        stg32(row + sre, sr, fr);
-                        stg32(row + sim, si, fi);
-                    } else {
-                        stg32(row + sre, fr, sr);
-                        stg32(row + sim, fi, si);
-                    }
-                }
-                if (!second && !lone) tc::tmem_st_wait();
-            }
-            sync_group();
         }
-    }
-    // drain copies still in flight (only after an abort), bounded
-    if (!ok && t == 0) {
-        if (pend0) tc::mbar_wait(bar_in0, ph_in0);
-        if (pend1) tc::mbar_wait(bar_in1, ph_in1);
+        if (ok && have_prev) {
+            sync_epi();  // the last unit's staging is complete
+            copy_out(prev);
+        }
+        if (issuer && last_mma >= 0) tc::mbar_wait(bar_mma2, (uint32_t)(last_mma & 1));
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -561,7 +665,7 @@ static mdt_status launch_tc(int ntaps, int mode, const ftc::Launch &L, cudaStrea
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return cuda_status(e, "fengine_tc: device query");
-    const long blocks = std::max(1L, std::min<long>(nsm, ((long)L.nwork + ftc::GROUPS - 1) / ftc::GROUPS));
+    const long blocks = std::max(1L, std::min<long>(nsm, (long)L.nwork));
     auto launch = [&](auto kern) -> mdt_status {
         cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)ftc::SMEM);

@@ -193,6 +193,22 @@ __device__ __forceinline__ void named_barrier(int id, int nthreads)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// Named barrier `id` over `nthreads` threads that also ORs `pred` over them:
+// every participating thread gets the same result.
+__device__ __forceinline__ bool named_barrier_or(int id, int nthreads, bool pred)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, %2, %3, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(id), "r"(nthreads)
+        : "memory");
+    return r != 0;
+}
+
 // Plain arrival (count 1) on an mbarrier.
 __device__ __forceinline__ void mbar_arrive(uint32_t bar)
 {
