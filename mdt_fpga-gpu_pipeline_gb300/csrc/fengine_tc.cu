@@ -20,10 +20,10 @@
 //
 // Work: one CTA per SM walks runs of up to 256 spectra of one element in
 // units of 8 spectra (two 128-row MMA tiles).  Warps 0-7 carry the last
-// Ntaps-1 converted input rows in registers, so every input sample is loaded
-// (bulk copy of 2 KB rows into a two-slot shared-memory ring) and converted
-// once; warps 8-15 run the twiddle and output stages of the previous unit
-// meanwhile (see fengine_tc_kernel).
+// Ntaps-1 converted input rows in tensor memory, so every input sample is
+// loaded (bulk copy of 2 KB rows into a two-slot shared-memory ring) and
+// converted once; warps 8-23 run the twiddle and output stages of the
+// previous unit meanwhile (see fengine_tc_kernel).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -38,10 +38,11 @@ namespace ftc {
 
 constexpr int N = 1024;
 constexpr int PT = 256;                 // PFB threads (warps 0-7)
-constexpr int ET = 256;                 // epilogue threads (warps 8-15)
+constexpr int ET = 512;                 // epilogue threads (warps 8-23)
 constexpr int THREADS = PT + ET;
 constexpr int US = 8;                   // spectra per unit
 constexpr int CPT = N / PT;             // channels per PFB thread
+constexpr int CPE = N / ET;             // channels per epilogue thread in the copy-out
 constexpr int ROWB = 2 * N;             // one (spectrum, element) row of int8 I/Q
 constexpr int RUN = 256;                // spectra per work item
 constexpr uint32_t TILE = 16384;        // 128 rows x 128 bytes
@@ -52,12 +53,14 @@ constexpr uint32_t OFF_B = 0, OFF_TW = 8192, OFF_QS = 16384, OFF_W = 20480;
 constexpr uint32_t OFF_P = 53248, OFF_Z = OFF_P + 4 * TILE, OFF_S = OFF_Z + 2 * TILE;
 constexpr uint32_t OFF_RING = OFF_S + 2 * TILE;
 constexpr uint32_t SMEM = OFF_RING + 2 * US * ROWB;
-// TMEM columns: MMA 1 accumulators (two buffers of two 64-column tiles), MMA 2
-// accumulators, then 64 columns holding the packed output of the first 8
-// spectra of each 16-spectrum pair
-constexpr uint32_t TMEM_COLS = 512, T_D1 = 0, T_D2 = 256, T_STASH = 384;
+// TMEM columns: two accumulator buffers of two 64-column tiles (MMA 1 of unit
+// u writes buffer u % 2, MMA 2 of the same unit overwrites it once the
+// twiddle stage has read it), 64 columns holding the packed output of the
+// first 8 spectra of each 16-spectrum pair, and the PFB carry: per PFB thread
+// and channel the last Ntaps-1 converted input rows (16 columns).
+constexpr uint32_t TMEM_COLS = 512, T_D = 0, T_STASH = 256, T_CARRY = 320;
 // mbarriers
-enum { BAR_RING = 0, BAR_MMA1 = 2, BAR_FREE1 = 4, BAR_MMA2 = 6, NBARS = 7 };
+enum { BAR_RING = 0, BAR_MMA1 = 2, BAR_FREE = 4, BAR_MMA2 = 6, NBARS = 7 };
 
 // One launch: a single job (with optional PFB history) or a device table of
 // jobs (FJob, work items from wk0).
@@ -247,13 +250,14 @@ struct OutUnit {
 };
 
 // Warp-specialised pipeline, one CTA per SM.  Warps 0-7 (PFB role) stream
-// the input, run the tap sum into P buffer u % 2 and issue MMA 1 into TMEM
-// D1 buffer u % 2.  Warps 8-15 (epilogue role) read D1, apply the twiddles
-// into Z, issue MMA 2, store the previous unit (from the staging buffer S)
+// the input, run the tap sum into P buffer u % 2 (the tap carry lives in
+// TMEM) and issue MMA 1 into TMEM accumulator buffer u % 2.  Warps 8-23
+// (epilogue role) read that buffer, apply the twiddles into Z, issue MMA 2
+// into the same buffer, store the previous unit (from the staging buffer S)
 // while MMA 2 works, then pack this unit's result into S.  The roles meet
-// only at mbarriers: MMA 1 done (P and D1 written / read) and D1 free
-// (epilogue has read D1), so the PFB of unit u + 1 runs while the epilogue
-// of unit u works.
+// only at mbarriers: MMA 1 done (P written, accumulators ready) and buffer
+// free (the epilogue has read MMA 2's result), so the PFB of unit u + 1 runs
+// while the epilogue of unit u works.
 template <int NT, int MODE>
 __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
 {
@@ -261,6 +265,7 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     __shared__ uint64_t bars[NBARS];
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
+    __shared__ OutUnit prev_s;  // the epilogue's staged unit awaiting its copy-out
 
     const uint32_t sbase = tc::smem_u32(sm);
     const int tid = threadIdx.x;
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
         for (int i = tid; i < N; i += THREADS) qs_s[i] = __ldg(L.qscales + i);
     if (tid == 0) {
         for (int b = 0; b < NBARS; b++)
-            tc::mbar_init(tc::smem_u32(&bars[b]), (b == BAR_FREE1 || b == BAR_FREE1 + 1) ? ET : 1);
+            tc::mbar_init(tc::smem_u32(&bars[b]), (b == BAR_FREE || b == BAR_FREE + 1) ? ET : 1);
         abort_flag = 0;
         tc::fence_mbar_init();
     }
@@ -321,7 +326,7 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     const uint32_t id_mma = tc::idesc_f16(64, 0, 0);  // M 128, N 64, f16 operands
     const uint64_t bdesc = tc::sw128_kmajor_desc(sbase + OFF_B);
     const uint32_t bar_mma1 = tc::smem_u32(&bars[BAR_MMA1]);    // + 8 * b
-    const uint32_t bar_free1 = tc::smem_u32(&bars[BAR_FREE1]);  // + 8 * b
+    const uint32_t bar_free = tc::smem_u32(&bars[BAR_FREE]);  // + 8 * b
     const uint32_t bar_mma2 = tc::smem_u32(&bars[BAR_MMA2]);
     const uint32_t gZ = sbase + OFF_Z;
 
@@ -337,10 +342,8 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
         bool pend0 = false, pend1 = false;  // loads in flight (for the drain on abort)
         const bool issuer = (t == 0);
         long last_mma = -1;
-        int cn1[CPT], cn2[CPT];
-#pragma unroll
-        for (int j = 0; j < CPT; j++) chan_of(8 * j + wg, l, cn1[j], cn2[j]);
-        uint64_t carry[CPT][NT - 1];
+        // carry of channel j: TMEM columns carry_t + 16 j (words 2i, 2i + 1 = row i)
+        const uint32_t carry_t = tmem + ((uint32_t)((wg & 3) * 32) << 16) + T_CARRY + (uint32_t)((wg >> 2) * 64);
         bool ok = true;
         long n = 0;  // units of this CTA so far
         FJob a = L.one;
@@ -389,11 +392,19 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
             pend1 = false;
 #pragma unroll
             for (int j = 0; j < CPT; j++) {
-                const uint32_t cb = (uint32_t)(2 * (32 * cn1[j] + cn2[j]));
+                int n1, n2;
+                chan_of(8 * j + wg, l, n1, n2);
+                const uint32_t cb = (uint32_t)(2 * (32 * n1 + n2));
+                uint32_t cv[16] = {};
 #pragma unroll
-                for (int i = 0; i < NT - 1; i++)
-                    carry[j][i] = iq_to_f2(lds_u16(gR + (uint32_t)(8 * ROWB + i * ROWB) + cb));
+                for (int i = 0; i < NT - 1; i++) {
+                    const float2 x = up2(iq_to_f2(lds_u16(gR + (uint32_t)(8 * ROWB + i * ROWB) + cb)));
+                    cv[2 * i] = __float_as_uint(x.x);
+                    cv[2 * i + 1] = __float_as_uint(x.y);
+                }
+                tc::tmem_st16(carry_t + (uint32_t)(16 * j), cv);
             }
+            tc::tmem_st_wait();
             if (sync_pfb_bad()) {
                 ok = false;
                 break;
@@ -419,8 +430,11 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                 // ---- PFB: 8 spectra x 4 channels per thread -> P tiles (f16, scaled)
 #pragma unroll
                 for (int j = 0; j < CPT; j++) {
-                    const int n1 = cn1[j], n2 = cn2[j];
+                    int n1, n2;
+                    chan_of(8 * j + wg, l, n1, n2);
                     const int c = 32 * n1 + n2;
+                    uint32_t cv[16];
+                    tc::tmem_ld16(carry_t + (uint32_t)(16 * j), cv);
                     uint64_t w2[NT];
 #pragma unroll
                     for (int pr = 0; pr < NT / 2; pr++) {
@@ -430,10 +444,12 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     }
                     uint64_t xw[NT - 1 + US];
 #pragma unroll
-                    for (int i = 0; i < NT - 1; i++) xw[i] = carry[j][i];
-#pragma unroll
                     for (int r = 0; r < US; r++)
                         xw[NT - 1 + r] = iq_to_f2(lds_u16(ring + (uint32_t)(r * ROWB + 2 * c)));
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int i = 0; i < NT - 1; i++)
+                        xw[i] = pk2(__uint_as_float(cv[2 * i]), __uint_as_float(cv[2 * i + 1]));
 #pragma unroll
                     for (int s = 0; s < US; s++) {
                         uint64_t acc = mul2(xw[s], w2[0]);
@@ -445,8 +461,14 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                                 pack_h2<__half>(p.x, p.y));
                     }
 #pragma unroll
-                    for (int i = 0; i < NT - 1; i++) carry[j][i] = xw[US + i];
+                    for (int i = 0; i < NT - 1; i++) {
+                        const float2 x = up2(xw[US + i]);
+                        cv[2 * i] = __float_as_uint(x.x);
+                        cv[2 * i + 1] = __float_as_uint(x.y);
+                    }
+                    tc::tmem_st16(carry_t + (uint32_t)(16 * j), cv);
                 }
+                tc::tmem_st_wait();  // the next unit reads the carry back
                 tc::fence_proxy_async();
                 if (sync_pfb_bad()) {
                     ok = false;
@@ -454,8 +476,8 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                 }
                 if (issuer) {
                     if (u + 2 < nunits) load_rows(slot, s0 + US * (u + 2) + NT - 1, unit_rows(u + 2), e);
-                    // D1 buffer b is free once the epilogue has read unit n - 2
-                    if (n >= 2 && !wait_or_abort(bar_free1 + 8 * b, (uint32_t)(((n >> 1) & 1) ^ 1), abortp)) {
+                    // accumulator buffer b is free once the epilogue has read unit n - 2
+                    if (n >= 2 && !wait_or_abort(bar_free + 8 * b, (uint32_t)(((n >> 1) & 1) ^ 1), abortp)) {
                         fail();
                     } else {
                         tc::fence_after_sync();
@@ -464,7 +486,7 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                             const uint64_t ad = tc::sw128_kmajor_desc(gP + (uint32_t)tl * TILE);
 #pragma unroll
                             for (int k = 0; k < 4; k++)
-                                tc::mma_f16(tmem + T_D1 + (uint32_t)(b * 128 + tl * 64), ad + 2 * k,
+                                tc::mma_f16(tmem + T_D + (uint32_t)(b * 128 + tl * 64), ad + 2 * k,
                                             bdesc + 2 * k, id_mma, k > 0);
                         }
                         tc::mma_commit(bar_mma1 + 8 * b);
@@ -488,13 +510,15 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
         }
     } else {
         // ======================================================= epilogue role
-        const int t = tid - PT, wg = t >> 5, l = t & 31;
-        const uint32_t lane_q = (uint32_t)((wg & 3) * 32) << 16;  // warp (8 + wg) reads lanes 32 (wg % 4) ..
-        const int tl = wg >> 2, qd = wg & 3;
-        const int su = tl * 4 + qd;  // spectrum of this thread's D1 / D2 rows within the unit
+        // 16 warps: warp 8 + ew reads TMEM lane quarter qd = ew % 4 of tile
+        // tl = (ew / 4) % 2, columns [32 hc, 32 hc + 32) with hc = ew / 8.
+        const int t = tid - PT, ew = t >> 5, l = t & 31;
+        const uint32_t lane_q = (uint32_t)((ew & 3) * 32) << 16;
+        const int qd = ew & 3, tl = (ew >> 2) & 1, hc = ew >> 3;
+        const int su = tl * 4 + qd;  // spectrum of this thread's accumulator rows within the unit
         const bool issuer = (t == 0);
         const uint32_t gS = sbase + OFF_S;
-        const uint32_t stash = tmem + lane_q + T_STASH + (uint32_t)(tl * 32);
+        const uint32_t stash = tmem + lane_q + T_STASH + (uint32_t)((ew >> 2) * 16);
         long last_mma = -1;
         bool ok = true;
         long n = 0;
@@ -507,21 +531,18 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
         // unit's packed 16-byte re and im chunks wait in TMEM, the second writes
         // both units' chunks as full 32-byte sectors (re chunks j, j+1 and im
         // chunks 4+j, 5+j of a row are sector neighbours under the row swizzle).
-        OutUnit prev{};
         bool have_prev = false;
-        auto copy_out = [&](const OutUnit &o) {
-            uint32_t p0[16];  // the first unit's words of two channels (second unit only)
+        auto copy_out = [&]() {
+            const OutUnit &o = prev_s;
             const bool stash_only = !o.second && !o.lone;
             const bool swap = (o.e & 1) != 0;  // the odd chunk comes first in the sector
             const uint32_t sre = (uint32_t)(((o.j0 ^ (o.e & 7)) & ~1) << 4);
             const uint32_t sim = (uint32_t)((((4 + o.j0) ^ (o.e & 7)) & ~1) << 4);
 #pragma unroll
-            for (int j = 0; j < CPT; j++) {
+            for (int j = 0; j < CPE; j++) {
                 const int c = t + ET * j;
-                if (o.second && (j & 1) == 0) {  // stash reads of channels j, j + 1
-                    tc::tmem_ld8(stash + (uint32_t)(8 * j), *reinterpret_cast<uint32_t(*)[8]>(p0));
-                    tc::tmem_ld8(stash + (uint32_t)(8 * j + 8), *reinterpret_cast<uint32_t(*)[8]>(p0 + 8));
-                }
+                uint32_t p0[8];  // the first unit's words (second unit only)
+                if (o.second) tc::tmem_ld8(stash + (uint32_t)(8 * j), p0);
                 uint32_t wv[US];
 #pragma unroll
                 for (int s = 0; s < US; s++)
@@ -541,8 +562,8 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     tc::tmem_st8(stash + (uint32_t)(8 * j), pk);
                     continue;
                 }
-                if (o.second && (j & 1) == 0) tc::tmem_ld_wait();
-                const uint32_t *fw = o.second ? p0 + 8 * (j & 1) : pk;  // first unit's words
+                if (o.second) tc::tmem_ld_wait();
+                const uint32_t *fw = o.second ? p0 : pk;  // first unit's words
                 const uint4 fr = make_uint4(fw[0], fw[1], fw[2], fw[3]);
                 const uint4 fi = make_uint4(fw[4], fw[5], fw[6], fw[7]);
                 const uint4 sr = o.second ? make_uint4(pk[0], pk[1], pk[2], pk[3]) : make_uint4(0u, 0u, 0u, 0u);
@@ -565,22 +586,20 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
             const int e = it.e, s0 = it.s0, nunits = it.nunits;
             for (int u = 0; u < nunits; u++, n++) {
                 const int b = (int)(n & 1);
-                // ---- twiddle: D1 (row = (spectrum, n2), col = k1) -> Z (row = (spectrum, k1), K = n2)
+                const uint32_t tacc = tmem + lane_q + T_D + (uint32_t)(b * 128 + tl * 64 + 32 * hc);
+                // ---- twiddle: MMA 1 result (row = (spectrum, n2), col = k1) -> Z (row = (spectrum, k1), K = n2)
                 if (!wait_or_abort(bar_mma1 + 8 * b, (uint32_t)((n >> 1) & 1), abortp)) fail();
                 tc::fence_after_sync();
                 {
-                    const uint32_t tbase = tmem + lane_q + T_D1 + (uint32_t)(b * 128 + tl * 64);
-                    uint32_t v[64];
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        tc::tmem_ld16(tbase + (uint32_t)(16 * q), *reinterpret_cast<uint32_t(*)[16]>(v + 16 * q));
+                    uint32_t v[32];
+                    tc::tmem_ld16(tacc, *reinterpret_cast<uint32_t(*)[16]>(v));
+                    tc::tmem_ld16(tacc + 16, *reinterpret_cast<uint32_t(*)[16]>(v + 16));
                     tc::tmem_ld_wait();
-                    tc::fence_before_sync();
-                    tc::mbar_arrive(bar_free1 + 8 * b);
                     const uint32_t abase = gZ + (uint32_t)tl * TILE;
 #pragma unroll
-                    for (int k1 = 0; k1 < 32; k1++) {
-                        const float yr = __uint_as_float(v[2 * k1]), yi = __uint_as_float(v[2 * k1 + 1]);
+                    for (int kk = 0; kk < 16; kk++) {
+                        const int k1 = 16 * hc + kk;
+                        const float yr = __uint_as_float(v[2 * kk]), yi = __uint_as_float(v[2 * kk + 1]);
                         const float2 tv = tw[k1 * 32 + l];
                         const float zr = fmaf(yr, tv.x, -yi * tv.y);
                         const float zi = fmaf(yr, tv.y, yi * tv.x);
@@ -588,64 +607,62 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     }
                 }
                 tc::fence_proxy_async();
+                tc::fence_before_sync();
                 if (sync_epi_bad()) {  // also orders the previous unit's staging before its copy-out
                     ok = false;
                     break;
                 }
-                if (issuer) {
+                if (issuer) {  // MMA 2 overwrites the accumulator buffer the twiddle stage has read
                     tc::fence_after_sync();
 #pragma unroll
                     for (int tt = 0; tt < 2; tt++) {
                         const uint64_t ad = tc::sw128_kmajor_desc(gZ + (uint32_t)tt * TILE);
 #pragma unroll
                         for (int k = 0; k < 4; k++)
-                            tc::mma_f16(tmem + T_D2 + (uint32_t)(tt * 64), ad + 2 * k, bdesc + 2 * k,
+                            tc::mma_f16(tmem + T_D + (uint32_t)(b * 128 + tt * 64), ad + 2 * k, bdesc + 2 * k,
                                         id_mma, k > 0);
                     }
                     tc::mma_commit(bar_mma2);
                     last_mma = n;
                 }
                 // ---- the previous unit's copy-out runs while MMA 2 works
-                if (have_prev) copy_out(prev);
-                // ---- output: D2 (row = (spectrum, k1), col = k2) -> staging S [channel][spectrum]
+                if (have_prev) copy_out();
+                // ---- output: MMA 2 result (row = (spectrum, k1), col = k2) -> staging S [channel][spectrum]
                 if (!wait_or_abort(bar_mma2, (uint32_t)(n & 1), abortp)) fail();
                 tc::fence_after_sync();
-                uint32_t v[64];
-                {
-                    const uint32_t tbase = tmem + lane_q + T_D2 + (uint32_t)(tl * 64);
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        tc::tmem_ld16(tbase + (uint32_t)(16 * q), *reinterpret_cast<uint32_t(*)[16]>(v + 16 * q));
-                    tc::tmem_ld_wait();
-                }
+                uint32_t v[32];
+                tc::tmem_ld16(tacc, *reinterpret_cast<uint32_t(*)[16]>(v));
+                tc::tmem_ld16(tacc + 16, *reinterpret_cast<uint32_t(*)[16]>(v + 16));
+                tc::tmem_ld_wait();
                 tc::fence_before_sync();
+                tc::mbar_arrive(bar_free + 8 * b);  // buffer b may take MMA 1 of unit n + 2
                 sync_epi();  // S is no longer read by the previous copy-out
 #pragma unroll
-                for (int kk = 0; kk < 32; kk++) {
-                    const int c = l + 32 * kk;
+                for (int kk = 0; kk < 16; kk++) {
+                    const int c = l + 32 * (16 * hc + kk);
                     const float qs = MODE == OUT_Q8 ? qs_s[c] : 1.0f;
                     sts_u32(gS + (uint32_t)(c * 32) + (uint32_t)((su ^ ((c >> 2) & 7)) << 2),
                             pack_out<MODE>(__uint_as_float(v[2 * kk]), __uint_as_float(v[2 * kk + 1]), qs));
                 }
-                {
+                if (issuer) {  // read by every epilogue thread after the next barrier
                     const int sabs = s0 + US * u;
                     const bool second = (u & 1) != 0;
                     const int s_first = second ? sabs - US : sabs;
-                    prev.X16 = a.X16;
-                    prev.nep = a.nep;
-                    prev.e = e;
-                    prev.kc = s_first >> 5;
-                    prev.j0 = (s_first & 31) >> 3;  // even
-                    prev.nvalid = min(US, a.nsp - sabs);
-                    prev.second = second;
-                    prev.lone = !second && u + 1 == nunits;  // first unit without a partner
-                    have_prev = true;
+                    prev_s.X16 = a.X16;
+                    prev_s.nep = a.nep;
+                    prev_s.e = e;
+                    prev_s.kc = s_first >> 5;
+                    prev_s.j0 = (s_first & 31) >> 3;  // even
+                    prev_s.nvalid = min(US, a.nsp - sabs);
+                    prev_s.second = second;
+                    prev_s.lone = !second && u + 1 == nunits;  // first unit without a partner
                 }
+                have_prev = true;
             }
         }
         if (ok && have_prev) {
             sync_epi();  // the last unit's staging is complete
-            copy_out(prev);
+            copy_out();
         }
         if (issuer && last_mma >= 0) tc::mbar_wait(bar_mma2, (uint32_t)(last_mma & 1));
     }
