@@ -42,7 +42,6 @@ constexpr int ET = 512;                 // epilogue threads (warps 8-23)
 constexpr int THREADS = PT + ET;
 constexpr int US = 8;                   // spectra per unit
 constexpr int CPT = N / PT;             // channels per PFB thread
-constexpr int CPE = N / ET;             // channels per epilogue thread in the copy-out
 constexpr int ROWB = 2 * N;             // one (spectrum, element) row of int8 I/Q
 constexpr int RUN = 256;                // spectra per work item
 constexpr uint32_t TILE = 16384;        // 128 rows x 128 bytes
@@ -536,45 +535,58 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
             const OutUnit &o = prev_s;
             const bool stash_only = !o.second && !o.lone;
             const bool swap = (o.e & 1) != 0;  // the odd chunk comes first in the sector
-            const uint32_t sre = (uint32_t)(((o.j0 ^ (o.e & 7)) & ~1) << 4);
-            const uint32_t sim = (uint32_t)((((4 + o.j0) ^ (o.e & 7)) & ~1) << 4);
+            // Lanes 2i and 2i+1 share a channel: lane 2i packs spectra 0-3 and
+            // writes the re sector, lane 2i+1 packs spectra 4-7 and writes the im
+            // sector, so each store instruction covers 16 rows (two sectors each)
+            // instead of 32.
+            const int hs = l & 1;
+            const uint32_t soff = hs ? (uint32_t)((((4 + o.j0) ^ (o.e & 7)) & ~1) << 4)
+                                     : (uint32_t)(((o.j0 ^ (o.e & 7)) & ~1) << 4);
+            const int nv = o.nvalid - 4 * hs;  // valid spectra of this lane's half
 #pragma unroll
-            for (int j = 0; j < CPE; j++) {
-                const int c = t + ET * j;
-                uint32_t p0[8];  // the first unit's words (second unit only)
-                if (o.second) tc::tmem_ld8(stash + (uint32_t)(8 * j), p0);
-                uint32_t wv[US];
+            for (int kp = 0; kp < 2; kp++) {
+                uint32_t p0[8];  // the first unit's chunks of rounds 2 kp, 2 kp + 1 (second unit only)
+                if (o.second) tc::tmem_ld8(stash + (uint32_t)(8 * kp), p0);
+                uint32_t q[8];  // this lane's 16-byte chunks of the unit, rounds 2 kp, 2 kp + 1
 #pragma unroll
-                for (int s = 0; s < US; s++)
-                    wv[s] = lds_u32(gS + (uint32_t)(c * 32) + (uint32_t)((s ^ ((c >> 2) & 7)) << 2));
-                if (o.nvalid < US) {
+                for (int kr = 0; kr < 2; kr++) {
+                    const int c = (t >> 1) + 256 * (2 * kp + kr);
+                    uint32_t w[4];
 #pragma unroll
-                    for (int s = 0; s < US; s++)
-                        if (s >= o.nvalid) wv[s] = 0u;
-                }
-                uint32_t pk[8];  // re (4 words: 8 spectra) then im
+                    for (int i = 0; i < 4; i++) {
+                        const int sp = 4 * hs + i;
+                        w[i] = lds_u32(gS + (uint32_t)(c * 32) + (uint32_t)((sp ^ ((c >> 2) & 7)) << 2));
+                    }
+                    if (nv < 4) {
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    pk[q] = __byte_perm(wv[2 * q], wv[2 * q + 1], 0x5410);
-                    pk[4 + q] = __byte_perm(wv[2 * q], wv[2 * q + 1], 0x7632);
+                        for (int i = 0; i < 4; i++)
+                            if (i >= nv) w[i] = 0u;
+                    }
+                    const uint32_t re0 = __byte_perm(w[0], w[1], 0x5410), re1 = __byte_perm(w[2], w[3], 0x5410);
+                    const uint32_t im0 = __byte_perm(w[0], w[1], 0x7632), im1 = __byte_perm(w[2], w[3], 0x7632);
+                    // lane 2i keeps re and sends im, lane 2i+1 keeps im and sends re
+                    const uint32_t x0 = __shfl_xor_sync(0xffffffffu, hs ? re0 : im0, 1);
+                    const uint32_t x1 = __shfl_xor_sync(0xffffffffu, hs ? re1 : im1, 1);
+                    q[4 * kr + 0] = hs ? x0 : re0;  // spectra 0-3, then 4-7, of this lane's component
+                    q[4 * kr + 1] = hs ? x1 : re1;
+                    q[4 * kr + 2] = hs ? im0 : x0;
+                    q[4 * kr + 3] = hs ? im1 : x1;
                 }
                 if (stash_only) {
-                    tc::tmem_st8(stash + (uint32_t)(8 * j), pk);
+                    tc::tmem_st8(stash + (uint32_t)(8 * kp), q);
                     continue;
                 }
                 if (o.second) tc::tmem_ld_wait();
-                const uint32_t *fw = o.second ? p0 : pk;  // first unit's words
-                const uint4 fr = make_uint4(fw[0], fw[1], fw[2], fw[3]);
-                const uint4 fi = make_uint4(fw[4], fw[5], fw[6], fw[7]);
-                const uint4 sr = o.second ? make_uint4(pk[0], pk[1], pk[2], pk[3]) : make_uint4(0u, 0u, 0u, 0u);
-                const uint4 si = o.second ? make_uint4(pk[4], pk[5], pk[6], pk[7]) : make_uint4(0u, 0u, 0u, 0u);
-                uint8_t *row = o.X16 + (((size_t)o.kc * N + c) * o.nep + o.e) * 128;
-                if (swap) {
-                    stg32(row + sre, sr, fr);
-                    stg32(row + sim, si, fi);
-                } else {
-                    stg32(row + sre, fr, sr);
-                    stg32(row + sim, fi, si);
+#pragma unroll
+                for (int kr = 0; kr < 2; kr++) {
+                    const int c = (t >> 1) + 256 * (2 * kp + kr);
+                    const uint32_t *fw = o.second ? p0 + 4 * kr : q + 4 * kr;  // first unit's chunk
+                    const uint4 f = make_uint4(fw[0], fw[1], fw[2], fw[3]);
+                    const uint4 sc = o.second ? make_uint4(q[4 * kr], q[4 * kr + 1], q[4 * kr + 2], q[4 * kr + 3])
+                                              : make_uint4(0u, 0u, 0u, 0u);
+                    uint8_t *row = o.X16 + (((size_t)o.kc * N + c) * o.nep + o.e) * 128;
+                    if (swap) stg32(row + soff, sc, f);
+                    else stg32(row + soff, f, sc);
                 }
             }
             if (stash_only) tc::tmem_st_wait();
