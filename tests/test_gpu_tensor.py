@@ -128,3 +128,22 @@ def test_tensor_plan_rejects_large_nch(mdt, cuda):
     with pytest.raises(mdt.MdtError) as e:
         mdt.FxPlan(16, 8192, 4, 64, precision=1)
     assert e.value.code == 2
+
+
+def test_tensor_path_deterministic(mdt, cuda):
+    """c3 shape: every sum of the tensor path has a fixed order, so two runs
+    agree bit for bit; the last channels agree with the FP32 path."""
+    cfg = mdt.configs.small(mdt.configs.C3, nspectra=512)
+    ne, nch, ntaps, nsp = cfg.nelements, cfg.nchannels, cfg.ntaps, cfg.nspectra
+    iq = gen(mdt, cfg, nsp + ntaps - 1)
+    win = window(mdt, nch, ntaps)
+    p1, v1 = run_plan(mdt, 1, ne, nch, ntaps, nsp, iq, win)
+    p2, v2 = run_plan(mdt, 1, ne, nch, ntaps, nsp, iq, win)
+    assert torch.equal(v1, v2)
+    p32, v32 = run_plan(mdt, 0, ne, nch, ntaps, nsp, iq, win)
+    tail = slice(nch - 64, nch)
+    err = rel_fro(v1[0, tail].cpu().numpy(), v32[0, tail].cpu().numpy().astype(np.complex128))
+    print("c3 shape, last 64 channels: f16 vs fp32 rel err %.3e" % err)
+    assert err < TOL_TC
+    for p in (p1, p2, p32):
+        p.close()
