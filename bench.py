@@ -47,7 +47,7 @@ NCU_TRAFFIC = {"fengine_c64b": 672.395008e6 + 2631.648e6,
 # captures at Nsp = 1024 (profiles/fengine_tc_c3.txt, profiles/xengine_tc_c3.txt):
 # the F-engine's reads and writes and the X-engine's operand reads grow with
 # the spectra processed, the X-engine's visibility writes do not.
-NCU_TRAFFIC_C3 = {"fengine_tc": 0.554507e9 * 8199 / 1031 + 1.032375e9 * 8,
+NCU_TRAFFIC_C3 = {"fengine_tc": 0.555248e9 * 8199 / 1031 + 1.022932e9 * 8,
                   "xengine_tc": 1.076980e9 * 8 + 0.484042e9}
 
 
