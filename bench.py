@@ -270,6 +270,42 @@ def measure_plan(mdt, cfg, precision, dev, steps, warmup, seed_offset=0):
     return ms, f_ms / max(count, 1), x_ms / max(count, 1), scale
 
 
+def f16_peaks(mdt, dev):
+    """Measured f16 tensor throughput on this GPU: tcgen05.mma kind::f16 with
+    its operands resident in shared memory, in the X-engine's instruction
+    shape (M128 N128, two CTAs per SM) and in the widest one (M128 N256, one
+    CTA per SM), and a cuBLAS fp16 GEMM (torch.matmul, 8192^3); each the best
+    of several runs on random operands."""
+    import torch
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    _, n128 = mdt.tc_peak_f16(128, 2, iters=20000, reps=5, err=err)
+    _, n256 = mdt.tc_peak_f16(256, 1, iters=20000, reps=5, err=err)
+    if int(err.item()) != 0:
+        raise RuntimeError("tc_peak_f16: a completion wait timed out")
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    a = torch.randn(8192, 8192, dtype=torch.float16, device=dev, generator=g)
+    b = torch.randn(8192, 8192, dtype=torch.float16, device=dev, generator=g)
+    for _ in range(3):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    best = float("inf")
+    for _ in range(10):
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    torch.cuda.empty_cache()
+    return {"tcgen05_kind_f16_m128n128_2cta_per_sm": n128,
+            "tcgen05_kind_f16_m128n256_1cta_per_sm": n256,
+            "cublas_fp16_gemm_8192": 2.0 * 8192 ** 3 / (best * 1e-3) / 1e12,
+            "unit": "TFLOP/s", "method": "best of several runs, random operands"}
+
+
 def tensor_path_section(mdt, dev, steps):
     """c3_array256 (NE=256, Nch=1024, Ntaps=8, Nsp=8192): the f16 tensor-core
     path (tensor-core F-engine + tensor-core X-engine) over the full 8
@@ -278,6 +314,7 @@ def tensor_path_section(mdt, dev, steps):
     with each kernel's roofline."""
     c3 = mdt.configs.C3
     hbm, bf16, kind = peaks()
+    pk = f16_peaks(mdt, dev)
     ms16, f16, x16, scale = measure_plan(mdt, c3, 1, dev, steps=steps, warmup=1)
     ms8, f8, x8, _ = measure_plan(mdt, c3, 3, dev, steps=max(1, steps // 2), warmup=1)
     c3_one = mdt.configs.small(c3, nint=1)
@@ -307,7 +344,9 @@ def tensor_path_section(mdt, dev, steps):
         "integrations": c3.nint, "fp32_path_value": v32, "speedup_vs_fp32_path": v16 / v32,
         "xengine_tc": {"ms_per_launch": x16, "tflops": x_tflops, "peak": bf16,
                        "frac": x_tflops / bf16, "peak_source": kind + " bf16_tflops (dense)",
+                       "frac_of_measured_kind_f16": x_tflops / pk["tcgen05_kind_f16_m128n128_2cta_per_sm"],
                        "algorithmic_flops": flops, "traffic": NCU_TRAFFIC_C3["xengine_tc"]},
+        "f16_peaks": pk,
         "fengine_tc": fe(f16, NCU_TRAFFIC_C3["fengine_tc"]),
         "fengine_simt_fft": fe(fsimt),
         "int8_path": {"value": v8, "unit": "antenna-samples/s", "ms_per_step": ms8,

@@ -182,6 +182,16 @@ MDT_API mdt_status mdt_fengine_tc_q8(int ne, int nch, int ntaps, int nsp, const 
                                      const float *window, void *X16, const float *qscales,
                                      int *err, cudaStream_t stream);
 
+/* Measured dense throughput of tcgen05.mma kind::f16 (M = 128, N = n of 128
+ * or 256, K = 16, FP32 accumulate, random f16 operands resident in shared
+ * memory): ctas_per_sm CTAs per SM (ctas_per_sm * n <= 512 TMEM columns),
+ * each issuing iters x 4 MMAs into one accumulator; the best of `reps` timed
+ * launches (after one warm-up) gives *best_ms and *tflops.  *err (device int)
+ * is set if the completion wait timed out.  Measurement support: the
+ * denominator for the X-engine's kind::f16 fraction. */
+MDT_API mdt_status mdt_tc_peak_f16(int n, int ctas_per_sm, int iters, int reps, float *best_ms,
+                                   double *tflops, int *err, cudaStream_t stream);
+
 /* Exact-int8 F-engine: as mdt_fengine_x16 but the values are integers
  * clamp(rint(x * qscales[c]), -127, 127) (stored as f16, exactly). */
 MDT_API mdt_status mdt_fengine_q8(int ne, int nch, int ntaps, int nsp, const int8_t *iq,

@@ -74,6 +74,8 @@ def _declare(L):
         "mdt_fengine_tc": ([_I, _I, _I, _I, _P, _P, _P, _I, _F, _P, _P], _I),
         "mdt_fengine_tc_q8": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P], _I),
         "mdt_fengine_q8": ([_I, _I, _I, _I, _P, _P, _P, _P, _P], _I),
+        "mdt_tc_peak_f16": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_float),
+                             ctypes.POINTER(ctypes.c_double), _P, _P], _I),
         "mdt_xengine_q8": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P], _I),
         "mdt_fx_integrate_static": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
         "mdt_fx_get_scale": ([_P, ctypes.POINTER(ctypes.c_float)], _I),
@@ -304,6 +306,16 @@ def fengine_tc(ne, nch, ntaps, nsp, iq, window, X16, err, ab_fmt=0, scale=1.0, s
     """Tensor-core F-engine (Nch 1024): same output layout as fengine_x16."""
     check(lib().mdt_fengine_tc(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X16), ab_fmt, scale,
                                ptr(err), stream_handle(stream)), "fengine_tc")
+
+
+def tc_peak_f16(n=256, ctas_per_sm=1, iters=20000, reps=5, err=None, stream=None):
+    """Measured kind::f16 tcgen05.mma throughput (best of `reps` launches):
+    (ms, TFLOP/s).  `err` is a device int32 tensor (a wait timeout sets it)."""
+    ms = ctypes.c_float(0.0)
+    tf = ctypes.c_double(0.0)
+    check(lib().mdt_tc_peak_f16(n, ctas_per_sm, iters, reps, ctypes.byref(ms), ctypes.byref(tf),
+                                ptr(err), stream_handle(stream)), "tc_peak_f16")
+    return ms.value, tf.value
 
 
 def fengine_tc_q8(ne, nch, ntaps, nsp, iq, window, X16, qscales, err, stream=None):

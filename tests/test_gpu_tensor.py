@@ -147,3 +147,16 @@ def test_tensor_path_deterministic(mdt, cuda):
     assert err < TOL_TC
     for p in (p1, p2, p32):
         p.close()
+
+
+def test_tc_peak_f16_microbenchmark(mdt, cuda):
+    """The kind::f16 tcgen05.mma throughput measurement runs, its completion
+    wait does not time out, and it lands between a tenth of the nominal 2.25
+    PFLOP/s dense figure and the 8192 flops per SM cycle at 2.07 GHz on 152 SMs
+    (2.58 PFLOP/s)."""
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for n, per_sm in ((256, 1), (128, 2)):
+        ms, tflops = mdt.tc_peak_f16(n, per_sm, iters=2000, reps=2, err=err)
+        print("kind::f16 M128 N%d, %d CTA/SM: %.1f TFLOP/s (%.3f ms)" % (n, per_sm, tflops, ms))
+        assert int(err.item()) == 0
+        assert 225.0 < tflops < 2580.0
