@@ -28,17 +28,16 @@
 // products are exact and an FP32 accumulator stays exact while every partial
 // sum is an integer below 2^24, i.e. for 16 K-chunks (512 spectra:
 // 512 * 2 * 127^2 < 2^24).  The MMAs therefore accumulate one 512-spectrum
-// window at a time into one of two TMEM window buffers; the epilogue warps
-// fold each finished window into int32 running sums kept in TMEM
-// (tcgen05.ld / tcgen05.st) while the MMAs fill the other buffer, and write
-// the exact int32 visibilities (and their scaled float values) at the end.
-// Column chunks are <= 64 wide: 2 windows x (Re, Im) + running (Re, Im) =
-// 6N <= 384 TMEM columns.
+// window at a time into one of two TMEM window buffers (2 x (Re, Im) x N =
+// 512 columns for N = 128); 16 epilogue warps fold each finished window into
+// int32 running sums held in their registers (a warp owns one TMEM lane
+// quarter and 32 columns) while the MMAs fill the other buffer, and write the
+// exact int32 visibilities (and their scaled float values) at the end.
 //
-// Warp roles (192 threads): warp 0 lane 0 issues bulk copies into a 4-stage
-// shared-memory ring; warp 1 allocates tensor memory and its lane 0 issues
-// the MMAs and commits; warps 2-5 read the accumulators (one TMEM lane
-// quarter each) and write visibilities.  Every mbarrier wait is bounded; a
+// Warp roles: warp 0 lane 0 issues bulk copies into the shared-memory stage
+// ring; warp 1 allocates tensor memory and its lane 0 issues the MMAs and
+// commits; the epilogue warps (2-5, or 2-17 in the exact int8 mode) read the
+// accumulators and write visibilities.  Every mbarrier wait is bounded; a
 // timeout sets the error flag and the block finishes without further work.
 #include <cstdlib>
 
@@ -52,6 +51,9 @@ constexpr int TC_STAGES = 4;
 constexpr int TC_BROWS = 256;  // max column-chunk rows (N)
 constexpr int TC_AROWS = 128;  // row tile (M)
 constexpr int TC_THREADS = 192;
+// threads of a KIND 0 block (producer, MMA, 4 epilogue warps) or a KIND 1
+// block (producer, MMA, 16 epilogue warps holding the int32 running sums)
+constexpr int tc_threads(int kind) { return kind == 1 ? 576 : TC_THREADS; }
 constexpr int TC_MAX_TILES = 160;
 constexpr uint32_t TC_B_BYTES = TC_BROWS * 128;
 constexpr uint32_t TC_A_BYTES = TC_AROWS * 128;
@@ -86,7 +88,7 @@ constexpr int TC_WIN = 16;  // K-chunks (of 32 spectra) per exact accumulation w
 // stages (one block per SM) or 128 with 3 stages (two blocks per SM, so one
 // block's epilogue overlaps the other's products).
 template <int KIND, int BROWS, int STAGES>  // KIND 0: f16 / bf16, float results; 1: exact int8
-__global__ void __launch_bounds__(TC_THREADS, (BROWS == 128 ? 2 : 1))
+__global__ void __launch_bounds__(tc_threads(KIND), (KIND == 0 && BROWS == 128 ? 2 : 1))
     xengine_tc_kernel(const __grid_constant__ TcArgs a)
 {
     constexpr uint32_t B_BYTES = BROWS * 128;
@@ -105,14 +107,14 @@ __global__ void __launch_bounds__(TC_THREADS, (BROWS == 128 ? 2 : 1))
     const int ch = blockIdx.x / a.ntiles;
     const TcTile tile = a.tiles[blockIdx.x - ch * a.ntiles];
     const int N = tile.n;
-    constexpr int NCOLMUL = (KIND == 0) ? 2 : 6;  // TMEM columns per output column
+    constexpr int NCOLMUL = (KIND == 0) ? 2 : 4;  // TMEM columns per output column
     const uint32_t ncols = (NCOLMUL * N <= 32) ? 32 : (NCOLMUL * N <= 64) ? 64
                          : (NCOLMUL * N <= 128) ? 128 : (NCOLMUL * N <= 256) ? 256 : 512;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < 2 * STAGES + 3; s++) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
-        tc::mbar_init(tc::smem_u32(&win_empty[0]), 4);  // one arrival per epilogue warp
-        tc::mbar_init(tc::smem_u32(&win_empty[1]), 4);
+        tc::mbar_init(tc::smem_u32(&win_empty[0]), 16);  // one arrival per epilogue warp
+        tc::mbar_init(tc::smem_u32(&win_empty[1]), 16);
         tc::fence_mbar_init();
     }
     if (warp == 1) {
@@ -200,75 +202,71 @@ __global__ void __launch_bounds__(TC_THREADS, (BROWS == 128 ? 2 : 1))
         tc::mma_commit(tc::smem_u32(&bars[2 * STAGES]));
         if (!ok) atomicExch(a.err, 1);
     } else if (warp >= 2 && KIND == 1) {
-        // ---------------- epilogue, exact int8 mode: fold windows into int32
-        const int quarter = warp & 3;
+        // ---------------- epilogue, exact int8 mode: 16 warps; warp w reads TMEM
+        // lane quarter w % 4, columns [32 cg, 32 cg + 32) with cg = (w - 2) / 4, and
+        // keeps the int32 running sums of its row and 32 columns in registers
+        const int quarter = warp & 3, cg = (warp - 2) >> 2;
         const int r = tile.r0 + quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
-        const uint32_t run_re = tmem + (uint32_t)(4 * N), run_im = tmem + (uint32_t)(5 * N);
         const int nwin = (a.nkc + TC_WIN - 1) / TC_WIN;
         float2 *Vc = a.V ? a.V + (long)ch * a.ne * a.ne : nullptr;
         double2 *Ac = a.Vacc ? a.Vacc + (long)ch * a.ne * a.ne : nullptr;
         int2 *Rc = a.raw ? a.raw + (long)ch * a.ne * a.ne : nullptr;
         const float qs = __ldg(a.qscales + ch);
         const float alpha = a.alpha / (qs * qs);
+        int rr[32], ri[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) rr[j] = ri[j] = 0;
         for (int w = 0; w < nwin; w++) {
             const int h = w & 1;
             ok = ok && tc::mbar_wait_sleep(tc::smem_u32(&win_full[h]), (w >> 1) & 1);
             tc::fence_after_sync();
             const uint32_t wre = tmem + (uint32_t)(h * 2 * N), wim = wre + (uint32_t)N;
-            const bool last = (w == nwin - 1);
-            for (int n0 = 0; n0 < N; n0 += 16) {
-                uint32_t vr[16], vi[16], rr[16], ri[16];
+#pragma unroll
+            for (int hf = 0; hf < 2; hf++) {
+                const int n0 = 32 * cg + 16 * hf;
+                if (n0 >= N) continue;  // warp-uniform
+                uint32_t vr[16], vi[16];
                 tc::tmem_ld16(wre + lane_off + n0, vr);
                 tc::tmem_ld16(wim + lane_off + n0, vi);
-                if (w > 0) {
-                    tc::tmem_ld16(run_re + lane_off + n0, rr);
-                    tc::tmem_ld16(run_im + lane_off + n0, ri);
-                }
                 tc::tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     // the window sums are integers below 2^24: exact in FP32
-                    const int xr = __float2int_rn(__uint_as_float(vr[j]));
-                    const int xi = __float2int_rn(__uint_as_float(vi[j]));
-                    rr[j] = (uint32_t)((w > 0 ? (int)rr[j] : 0) + xr);
-                    ri[j] = (uint32_t)((w > 0 ? (int)ri[j] : 0) + xi);
-                }
-                if (!last) {
-                    tc::tmem_st16(run_re + lane_off + n0, rr);
-                    tc::tmem_st16(run_im + lane_off + n0, ri);
-                } else if (ok && r < a.ne) {
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const int q = tile.q0 + n0 + j;
-                        if (q >= a.ne || q > r) continue;
-                        const int ire = (int)rr[j];
-                        const int iim = (q == r) ? 0 : (int)ri[j];
-                        const long lo = (long)q * a.ne + r, up = (long)r * a.ne + q;
-                        if (Rc) {
-                            Rc[lo] = make_int2(ire, iim);
-                            if (q != r) Rc[up] = make_int2(ire, -iim);
-                        }
-                        const float re = (float)ire * alpha, im = (float)iim * alpha;
-                        if (Vc) {
-                            Vc[lo] = make_float2(re, im);
-                            if (q != r) Vc[up] = make_float2(re, -im);
-                        }
-                        if (Ac) {
-                            double2 x = Ac[lo];
-                            Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
-                            if (q != r) {
-                                double2 y = Ac[up];
-                                Ac[up] = make_double2(y.x + (double)re, y.y - (double)im);
-                            }
-                        }
-                    }
+                    rr[16 * hf + j] += __float2int_rn(__uint_as_float(vr[j]));
+                    ri[16 * hf + j] += __float2int_rn(__uint_as_float(vi[j]));
                 }
             }
-            if (!last) tc::tmem_st_wait();
             tc::fence_before_sync();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(tc::smem_u32(&win_empty[h]));
+        }
+        if (ok && r < a.ne) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int q = tile.q0 + 32 * cg + j;
+                if (32 * cg + j >= N || q >= a.ne || q > r) continue;
+                const int ire = rr[j];
+                const int iim = (q == r) ? 0 : ri[j];
+                const long lo = (long)q * a.ne + r, up = (long)r * a.ne + q;
+                if (Rc) {
+                    Rc[lo] = make_int2(ire, iim);
+                    if (q != r) Rc[up] = make_int2(ire, -iim);
+                }
+                const float re = (float)ire * alpha, im = (float)iim * alpha;
+                if (Vc) {
+                    Vc[lo] = make_float2(re, im);
+                    if (q != r) Vc[up] = make_float2(re, -im);
+                }
+                if (Ac) {
+                    double2 x = Ac[lo];
+                    Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
+                    if (q != r) {
+                        double2 y = Ac[up];
+                        Ac[up] = make_double2(y.x + (double)re, y.y - (double)im);
+                    }
+                }
+            }
         }
         if (!ok && lane == 0) atomicExch(a.err, 1);
     } else if (warp >= 2 && KIND == 0) {
@@ -591,15 +589,15 @@ mdt_status xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qs
     a.err = err;
     a.qscales = qscales;
     a.raw = raw;
-    a.ntiles = make_tiles(ne, a.nep, 64, a.tiles);
+    a.ntiles = make_tiles(ne, a.nep, 128, a.tiles);
     if (a.ntiles <= 0) return invalid("xengine_q8: too many tiles");
-    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<1, 256, 4>,
+    cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<1, 128, 4>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)tc_smem(256, 4));
+                                         (int)tc_smem(128, 4));
     if (e != cudaSuccess) return cuda_status(e, "xengine_q8 smem attribute");
     long blocks = (long)nch * a.ntiles;
     if (blocks > 0x7fffffffL) return invalid("xengine_q8: grid too large");
-    xengine_tc_kernel<1, 256, 4><<<(unsigned)blocks, TC_THREADS, tc_smem(256, 4), stream>>>(a);
+    xengine_tc_kernel<1, 128, 4><<<(unsigned)blocks, tc_threads(1), tc_smem(128, 4), stream>>>(a);
     return launch_status("xengine_tc_kernel<exact int8>");
 }
 
