@@ -173,7 +173,9 @@ struct FengBCfg {
     static constexpr int MINB =
         (MDT_FENG16_SM_THREADS / THREADS) < 1 ? 1 : (MDT_FENG16_SM_THREADS / THREADS);
     static constexpr int RSTRIDE = fft::Shape<N>::PADN + 4;
-    static constexpr size_t SMEM = sizeof(float2) * (size_t)RSTRIDE * SB8;
+    // the transform's rows, then the block's int8 input rows (up to 8 + 7)
+    static constexpr size_t STAGE_OFF = (sizeof(float2) * (size_t)RSTRIDE * SB8 + 15) / 16 * 16;
+    static constexpr size_t SMEM = STAGE_OFF + (size_t)(SB8 + 7) * 2 * N;
 };
 
 template <int CPI>
@@ -181,6 +183,12 @@ struct Samples;
 template <>
 struct Samples<1> {
     float re[1], im[1];
+    __device__ __forceinline__ void load_shared(const uint8_t *p)
+    {
+        const char2 v = *reinterpret_cast<const char2 *>(p);
+        re[0] = (float)v.x;
+        im[0] = (float)v.y;
+    }
     __device__ __forceinline__ void load(const char2 *p, bool ok)
     {
         const char2 v = ok ? __ldg(p) : make_char2(0, 0);
@@ -191,6 +199,14 @@ struct Samples<1> {
 template <>
 struct Samples<2> {
     float re[2], im[2];
+    __device__ __forceinline__ void load_shared(const uint8_t *p)
+    {
+        const char4 v = *reinterpret_cast<const char4 *>(p);
+        re[0] = (float)v.x;
+        im[0] = (float)v.y;
+        re[1] = (float)v.z;
+        im[1] = (float)v.w;
+    }
     __device__ __forceinline__ void load(const char2 *p, bool ok)
     {
         const char4 v = ok ? __ldg(reinterpret_cast<const char4 *>(p)) : make_char4(0, 0, 0, 0);
@@ -201,14 +217,42 @@ struct Samples<2> {
     }
 };
 
+// 16-byte asynchronous global->shared copy; src_bytes 0 fills zeros.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+
+// The block's input rows (spectra s0 .. s0+7+NT-1 of element e) are first
+// copied into shared memory `stage` with cp.async, all in flight at once
+// (rows past the input are zero-filled); the tap sum then reads them there.
 template <int N, int NT, int THREADS>
 __device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, int e, float2 *smem,
-                                                   int rstride)
+                                                   int rstride, uint8_t *stage)
 {
     constexpr int CPI = (N / THREADS >= 2) ? 2 : 1;  // channels per thread item
     constexpr int ITEMS = N / CPI;
+    constexpr int NROW = SB8 + NT - 1;
+    constexpr int RCHUNKS = 2 * N / 16;  // 16-byte chunks per input row
     const long rowlen = (long)a.ne * N;
     const int nin = a.nsp + NT - 1;  // input spectra of this integration
+    for (int i = threadIdx.x; i < NROW * RCHUNKS; i += THREADS) {
+        const int j = i / RCHUNKS, k = i - j * RCHUNKS;
+        const int sp = s0 + j;
+        const char2 *row = (sp < a.nhist) ? a.hist + (long)sp * rowlen
+                                          : a.iq + (long)(sp - a.nhist) * rowlen;
+        const bool in = sp < nin;
+        cp_async16(stage + (size_t)j * 2 * N + 16 * k,
+                   in ? reinterpret_cast<const uint8_t *>(row + (long)e * N) + 16 * k
+                      : reinterpret_cast<const uint8_t *>(a.iq),
+                   in ? 16 : 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
     for (int it = threadIdx.x; it < ITEMS; it += THREADS) {
         const int c0 = it * CPI;
         float w[NT][CPI];
@@ -223,11 +267,8 @@ __device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, in
             for (int k = 0; k < CPI; k++) ar[r][k] = ai[r][k] = 0.0f;
 #pragma unroll
         for (int j = 0; j < SB8 + NT - 1; j++) {
-            const int sp = s0 + j;
-            const char2 *src = (sp < a.nhist) ? a.hist + (long)sp * rowlen
-                                              : a.iq + (long)(sp - a.nhist) * rowlen;
             Samples<CPI> x;
-            x.load(src + (long)e * N + c0, sp < nin);
+            x.load_shared(stage + (size_t)j * 2 * N + 2 * c0);
 #pragma unroll
             for (int r = 0; r < SB8; r++) {
                 const int i = j - r;
@@ -272,7 +313,8 @@ __device__ __forceinline__ void fengine_block8(const FengArgs &a, const Block8 &
 {
     using C = FengBCfg<N>;
     if constexpr (NT > 0)
-        pfb_block8_to_smem<N, NT, C::THREADS>(a, b.s0, b.e, fsm, C::RSTRIDE);
+        pfb_block8_to_smem<N, NT, C::THREADS>(a, b.s0, b.e, fsm, C::RSTRIDE,
+                                              reinterpret_cast<uint8_t *>(fsm) + C::STAGE_OFF);
     else
         pfb_rows_to_smem<N, SB8, C::THREADS, true>(a, b.s0, b.e, fsm, C::RSTRIDE);
     __syncthreads();
