@@ -1,7 +1,7 @@
 /*
  * mdt_oracle.c -- the oracle: a plain-C CPU restatement of the reference's
- * GPU FX correlator hot path (aragorn2101/MDT_FPGA-GPU_pipeline), used ONLY as
- * the checker by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * GPU FX correlator hot path (aragorn2101/MDT_FPGA-GPU_pipeline), used ONLY to
+ * check results in tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
  * leg. The product library never links, loads or calls it.
  *
  * Parity pins: the bit-exact functions (pps_f32_exact, reorder_c64) are checked

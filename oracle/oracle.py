@@ -1,8 +1,8 @@
 """ctypes binding of the oracle (oracle/mdt_oracle.c).
 
-TEST INFRASTRUCTURE ONLY. The oracle is the checker: tests/, the smoke check
-in __graft_entry__ and the CPU-baseline leg of bench.py use it; the product
-library never does.
+TEST INFRASTRUCTURE ONLY. Results are checked against the oracle in tests/,
+the smoke check in __graft_entry__ and the CPU-baseline leg of bench.py; the
+product library never uses it.
 
 build() compiles the C restatement into oracle/_build/libmdt_oracle.so with
 gcc/cc (-fopenmp, -ffp-contract=off).  Every function takes numpy arrays and

@@ -1,4 +1,4 @@
-"""The FP64 checkers of the adjoint tests agree with each other (CPU only):
+"""The FP64 references of the adjoint tests agree with each other (CPU only):
 the PyTorch float64 forward equals the FP64 oracle's FX pipeline, and its
 autograd gradient equals FP64 central finite differences of the oracle."""
 import numpy as np
