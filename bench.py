@@ -495,7 +495,7 @@ def run_ours(args, cfg):
     mdt.window_hamming_sinc(nch, ntaps, win)
     vis = torch.empty(nint, nch, ne, ne, dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
-    prec = {"fp32": 0, "fp16": 1, "bf16": 2}[args.precision]
+    prec = {"fp32": 0, "fp16": 1, "bf16": 2, "int8": 3}[args.precision]
     plan = mdt.FxPlan(ne, nch, ntaps, nsp, precision=prec, stream=stream)
     plan.set_window(win)
 
@@ -641,7 +641,8 @@ def run_ours(args, cfg):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp32": "f32", "fp16": "f16 operands / f32 accumulate",
-                      "bf16": "bf16 operands / f32 accumulate"}[args.precision],
+                      "bf16": "bf16 operands / f32 accumulate",
+                      "int8": "int8 F-output / exact int32 sums"}[args.precision],
             "data": "synthetic (seeded integer int8 I/Q generator)",
             "config": {"workload": cfg.name, "nelements": ne, "nchannels": nch, "ntaps": ntaps,
                        "nspectra": nsp, "integrations": nint,
@@ -678,7 +679,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the c4 ragged-batch section")
     ap.add_argument("--no-tensor", action="store_true",
                     help="skip the c3 tensor-core vs FP32 section")
-    ap.add_argument("--precision", choices=["fp32", "fp16", "bf16"], default="fp32",
+    ap.add_argument("--precision", choices=["fp32", "fp16", "bf16", "int8"], default="fp32",
                     help="plan precision of the main measurement")
     ap.add_argument("--nspectra", type=int, default=None,
                     help="override spectra per integration (small profiling cases)")
