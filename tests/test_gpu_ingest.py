@@ -19,7 +19,7 @@ def dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def run_case(mdt, oracle, ne, nch, ntaps, nsp, nint, sper, formatted, seed):
+def run_case(mdt, oracle, ne, nch, ntaps, nsp, nint, sper, formatted, seed, precision=0):
     rng = np.random.default_rng(seed)
     fd = fmt_dict(sper, bits=8)
     S = nsp * nint + ntaps - 1
@@ -54,7 +54,8 @@ def run_case(mdt, oracle, ne, nch, ntaps, nsp, nint, sper, formatted, seed):
     mdt.window_hamming_sinc(nch, ntaps, win)
     fmt = mdt.packet_format(sper, fd["inputs_per_snap"], fd["inputs_per_station"],
                             fd["words_header"], 8, fd["packet_bytes"])
-    ing = mdt.Ingest(ne, nch, ntaps, nsp, fmt, max_packets=64, formatted=formatted)
+    ing = mdt.Ingest(ne, nch, ntaps, nsp, fmt, max_packets=64, formatted=formatted,
+                     precision=precision)
     ing.set_window(win)
     results = {}
     stats = {}
@@ -90,7 +91,7 @@ def run_case(mdt, oracle, ne, nch, ntaps, nsp, nint, sper, formatted, seed):
     assert cnt["late"] == 1 and cnt["bad"] == 0
     assert sorted(results) == list(range(nint))
     # expected: the plan over the same samples with the dropped ones zero
-    plan = mdt.FxPlan(ne, nch, ntaps, nsp)
+    plan = mdt.FxPlan(ne, nch, ntaps, nsp, precision=precision)
     plan.set_window(win)
     vis = torch.empty(nint, nch, ne, ne, dtype=torch.complex64, device="cuda")
     plan.execute(dev(zero.reshape(-1)), nint, vis)
@@ -112,6 +113,13 @@ def run_case(mdt, oracle, ne, nch, ntaps, nsp, nint, sper, formatted, seed):
 def test_ingest_stream_matches_plan(mdt, cuda, oracle, formatted):
     run_case(mdt, oracle, ne=38, nch=256, ntaps=4, nsp=64, nint=6, sper=32,
              formatted=formatted, seed=3 + formatted)
+
+
+def test_ingest_tensor_path_graphs(mdt, cuda, oracle):
+    # f16 tensor path at Nch 1024: the tensor-core F-engine and X-engine run
+    # eagerly for two windows, then from graphs replayed per buffer parity
+    run_case(mdt, oracle, ne=38, nch=1024, ntaps=8, nsp=64, nint=4, sper=32, formatted=False,
+             seed=21, precision=1)
 
 
 def test_ingest_packets_straddling_windows(mdt, cuda, oracle):
