@@ -3,8 +3,8 @@
 // cufftExecC2C replacement) and by the fused F-engine.
 //
 // One row of N = 2^L complex values is transformed by TPR threads through
-// L/3 radix-8 passes and, when L is not a multiple of 3, one final radix-2
-// or radix-4 pass.  Pass p (radix R, NS = 8^p) on butterfly b:
+// L/4 radix-16 passes and, when L is not a multiple of 4, one final radix-2,
+// radix-4 or radix-8 pass.  Pass p (radix R, NS = 16^p) on butterfly b:
 //   v[m]  = x[b + m*N/R]                              m = 0..R-1
 //   v[m] *= exp(-2 pi i m (b mod NS) / (NS*R))        (table lookup)
 //   v     = DFT_R(v)
@@ -32,16 +32,16 @@ namespace mdt {
 namespace fft {
 
 constexpr int clog2(int n) { return n <= 1 ? 0 : 1 + clog2(n / 2); }
-constexpr int ipow8(int p) { return p == 0 ? 1 : 8 * ipow8(p - 1); }
+constexpr int ipow16(int p) { return p == 0 ? 1 : 16 * ipow16(p - 1); }
 
 __host__ __device__ constexpr int pad(int i) { return i + (i >> 4); }
 
 template <int N>
 struct Shape {
     static constexpr int L = clog2(N);
-    static constexpr int P8 = L / 3;     // radix-8 passes
-    static constexpr int REM = L % 3;    // final radix-2^REM pass if REM > 0
-    static constexpr int NPASS = P8 + (REM ? 1 : 0);
+    static constexpr int P16 = L / 4;    // radix-16 passes
+    static constexpr int REM = L % 4;    // final radix-2^REM pass if REM > 0
+    static constexpr int NPASS = P16 + (REM ? 1 : 0);
     static constexpr int TPR = (N / 8 < 1) ? 1 : ((N / 8 > 1024) ? 1024 : N / 8);  // threads per row
     static constexpr int PADN = pad(N);  // float2 slots of one padded row
 };
@@ -103,6 +103,50 @@ __device__ __forceinline__ void dft<8>(float2 *v)
     v[1] = b0; v[3] = b1; v[5] = b2; v[7] = b3;
 }
 
+// v * (1 - i)/sqrt2 and v * (-1 - i)/sqrt2 (W16^2 and W16^6)
+__device__ __forceinline__ float2 mul_w8(float2 b)
+{
+    return make_float2(__fmul_rn(__fadd_rn(b.x, b.y), kRsqrt2), __fmul_rn(__fsub_rn(b.y, b.x), kRsqrt2));
+}
+__device__ __forceinline__ float2 mul_w8_3(float2 b)
+{
+    return make_float2(__fmul_rn(__fsub_rn(b.y, b.x), kRsqrt2), -__fmul_rn(__fadd_rn(b.x, b.y), kRsqrt2));
+}
+
+// cos(pi/8), sin(pi/8)
+constexpr float kC16 = 0.92387953251128675613f, kS16 = 0.38268343236508977173f;
+
+// Radix-16 as 4 x 4: DFT4 over m1 of v[m2 + 4 m1] for each m2, twiddles
+// W16^(m2 q), DFT4 over m2 for each q; output k = q + 4 r is left in
+// position 4 q + r and moved to natural order at the end.
+template <>
+__device__ __forceinline__ void dft<16>(float2 *v)
+{
+#pragma unroll
+    for (int m2 = 0; m2 < 4; m2++) dft4v(v[m2], v[m2 + 4], v[m2 + 8], v[m2 + 12]);
+    // v[m2 + 4 q] *= W16^(m2 q),  W16^k = cos(k pi/8) - i sin(k pi/8)
+    const float2 w1 = make_float2(kC16, -kS16), w3 = make_float2(kS16, -kC16),
+                 w9 = make_float2(-kC16, kS16);
+    v[1 + 4] = cmul(v[1 + 4], w1);      // m2 1, q 1: W^1
+    v[1 + 8] = mul_w8(v[1 + 8]);        // m2 1, q 2: W^2
+    v[1 + 12] = cmul(v[1 + 12], w3);    // m2 1, q 3: W^3
+    v[2 + 4] = mul_w8(v[2 + 4]);        // m2 2, q 1: W^2
+    v[2 + 8] = cmul_mi(v[2 + 8]);       // m2 2, q 2: W^4 = -i
+    v[2 + 12] = mul_w8_3(v[2 + 12]);    // m2 2, q 3: W^6
+    v[3 + 4] = cmul(v[3 + 4], w3);      // m2 3, q 1: W^3
+    v[3 + 8] = mul_w8_3(v[3 + 8]);      // m2 3, q 2: W^6
+    v[3 + 12] = cmul(v[3 + 12], w9);    // m2 3, q 3: W^9
+#pragma unroll
+    for (int q = 0; q < 4; q++) dft4v(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    float2 y[16];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) y[q + 4 * r] = v[4 * q + r];
+#pragma unroll
+    for (int k = 0; k < 16; k++) v[k] = y[k];
+}
+
 // One Stockham pass over one row.  `t` is the thread's index within the row
 // (0..TPR-1); every thread of the block must call every pass (barriers).
 // LOADFN (pass 0 only): inputs come from load(i) instead of shared memory,
@@ -115,8 +159,8 @@ __device__ __forceinline__ void stockham_pass(float2 *sx, int t,
                                               const float2 *__restrict__ tw, Load &load,
                                               Store &store)
 {
-    constexpr int R = (P < Shape<N>::P8) ? 8 : (1 << Shape<N>::REM);
-    constexpr int NS = ipow8(P);
+    constexpr int R = (P < Shape<N>::P16) ? 16 : (1 << Shape<N>::REM);
+    constexpr int NS = ipow16(P);
     constexpr int NB = N / R;
     constexpr int NBT = (NB + TPR - 1) / TPR;
     float2 v[NBT][R];
@@ -150,6 +194,27 @@ __device__ __forceinline__ void stockham_pass(float2 *sx, int t,
                     v[k][5] = cmul(v[k][5], cmul(w1, w4));
                     v[k][6] = cmul(v[k][6], cmul(w2, w4));
                     v[k][7] = cmul(v[k][7], cmul(w3, w4));
+                } else if constexpr (R == 16) {
+                    // radix 16: w, w^2, w^4, w^8 from the table, the others as products
+                    const float2 w1 = __ldg(&tw[jm * TS]), w2 = __ldg(&tw[2 * jm * TS]),
+                                 w4 = __ldg(&tw[4 * jm * TS]), w8 = __ldg(&tw[8 * jm * TS]);
+                    const float2 w3 = cmul(w1, w2), w5 = cmul(w1, w4), w6 = cmul(w2, w4),
+                                 w7 = cmul(w3, w4);
+                    v[k][1] = cmul(v[k][1], w1);
+                    v[k][2] = cmul(v[k][2], w2);
+                    v[k][3] = cmul(v[k][3], w3);
+                    v[k][4] = cmul(v[k][4], w4);
+                    v[k][5] = cmul(v[k][5], w5);
+                    v[k][6] = cmul(v[k][6], w6);
+                    v[k][7] = cmul(v[k][7], w7);
+                    v[k][8] = cmul(v[k][8], w8);
+                    v[k][9] = cmul(v[k][9], cmul(w1, w8));
+                    v[k][10] = cmul(v[k][10], cmul(w2, w8));
+                    v[k][11] = cmul(v[k][11], cmul(w3, w8));
+                    v[k][12] = cmul(v[k][12], cmul(w4, w8));
+                    v[k][13] = cmul(v[k][13], cmul(w5, w8));
+                    v[k][14] = cmul(v[k][14], cmul(w6, w8));
+                    v[k][15] = cmul(v[k][15], cmul(w7, w8));
                 } else
 #endif
                 {
