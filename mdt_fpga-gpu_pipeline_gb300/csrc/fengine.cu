@@ -38,8 +38,8 @@ namespace mdt {
 #define MDT_FENG_SM_THREADS 1024
 #endif
 
-// Threads per row: N/8 (one radix-8 butterfly each) capped at `cap`, but
-// never fewer than N/16 (at most two butterflies per thread and pass).
+// Threads per row: N/8 capped at `cap`, but never fewer than N/16 (at most
+// one radix-16 or two radix-8 butterflies per thread and pass).
 constexpr int feng_tpr(int n, int cap)
 {
     return (n / 8 < 1) ? 1 : (n / 8 <= cap ? n / 8 : (cap >= n / 16 ? cap : n / 16));

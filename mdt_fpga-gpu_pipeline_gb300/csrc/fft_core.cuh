@@ -22,8 +22,9 @@
 #pragma once
 #include "mdt_common.cuh"
 
-// Radix-8 twiddles: 0 = seven table loads per butterfly; 1 = three loads and
-// four complex products (fewer load instructions, a few ulp more rounding).
+// Radix-8 / radix-16 twiddles: 0 = one table load per power; 1 = loads of
+// w, w^2, w^4 (and w^8) and the other powers as complex products (fewer load
+// instructions, a few ulp more rounding).
 #ifndef MDT_FFT_TW_PRODUCTS
 #define MDT_FFT_TW_PRODUCTS 1
 #endif
