@@ -28,7 +28,11 @@ constexpr int XS_ST = 64;       // super-tile width
 constexpr int XS_MT = 4;        // micro-tile width
 constexpr int XS_KC = 32;       // time samples staged per chunk
 constexpr int XS_THREADS = 256;
-constexpr int XS_RS = XS_ST + 2;  // staged row stride (float2): 16-byte aligned rows, bank skew
+// Staged operand rows are element-major: row e holds the chunk's XS_KC time
+// samples as XS_KC/2 16-byte pairs; pair j of row e sits at position
+// j ^ ((e / XS_MT) & 7), so the 16-byte loads of lanes with different
+// micro-tile rows fall in different bank groups.
+constexpr int XS_ROWB = XS_KC * 8;  // bytes per staged row
 
 struct XengArgs {
     int ne, nsp, nsuper, npairs;
@@ -63,19 +67,33 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_by
                  "l"(src), "r"(src_bytes)
                  : "memory");
 }
+// 16-byte asynchronous global->shared copy; src_bytes 0 fills zeros.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-constexpr size_t XS_SMEM = sizeof(float2) * 2 /*stages*/ * 2 /*A,B*/ * XS_KC * XS_RS;
+constexpr size_t XS_SMEM = (size_t)2 /*stages*/ * 2 /*A,B*/ * XS_ST * XS_ROWB;
+
+// byte offset of time sample kk of element e in a staged operand
+__device__ __forceinline__ int xs_off(int e, int kk)
+{
+    return e * XS_ROWB + ((((kk >> 1) ^ ((e >> 2) & 7))) << 4) + ((kk & 1) << 3);
+}
 
 __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArgs a)
 {
     // [stage][operand][k][element]; the K-slice reduction reuses the space
     extern __shared__ float4 xs_smem4[];
     float2 *sbuf = reinterpret_cast<float2 *>(xs_smem4);
-    auto tileA = [&](int st) { return sbuf + (size_t)(st * 2 + 0) * XS_KC * XS_RS; };
-    auto tileB = [&](int st) { return sbuf + (size_t)(st * 2 + 1) * XS_KC * XS_RS; };
+    auto tileA = [&](int st) { return reinterpret_cast<uint8_t *>(sbuf) + (size_t)(st * 2 + 0) * XS_ST * XS_ROWB; };
+    auto tileB = [&](int st) { return reinterpret_cast<uint8_t *>(sbuf) + (size_t)(st * 2 + 1) * XS_ST * XS_ROWB; };
 
     // dual mode (single diagonal super-tile per channel): channels 2b and
     // 2b+1, staged into the A and B buffers; otherwise one (channel, pair)
@@ -90,7 +108,7 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     const int nmr = (nr + XS_MT - 1) / XS_MT, nmq = (nq + XS_MT - 1) / XS_MT;
     const int nmt = diag ? nmr * (nmr + 1) / 2 : nmr * nmq;
     const int nmt2 = a.dual ? 2 * nmt : nmt;  // micro-tiles of the block
-    const int ksl = min(XS_KC, max(1, XS_THREADS / nmt2));
+    const int ksl = min(XS_KC / 2, max(1, XS_THREADS / nmt2));  // K slices (of sample pairs)
     const int tid = threadIdx.x;
     const int mt2 = tid % nmt2, ks = tid / nmt2;
     const int cs = mt2 / nmt, mt = mt2 - cs * nmt;  // channel slot (dual), micro-tile
@@ -106,34 +124,42 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     const float2 *Xc = a.Xptrs ? a.Xptrs[ch] : a.X + (long)ch * a.xstride;
     const float2 *Xc2 = !has2 ? Xc : (a.Xptrs ? a.Xptrs[ch + 1] : a.X + (long)(ch + 1) * a.xstride);
 
-    // stage chunk k0 into buffer st: XS_KC x 64 complex per operand, [kk][e]
+    // stage chunk k0 into buffer st: 64 element rows of XS_KC samples per operand
     auto stage = [&](int k0, int st) {
-        float2 *A = tileA(st), *B = tileB(st);
-        for (int idx = tid; idx < XS_KC * XS_ST; idx += XS_THREADS) {
-            int kk, e;
-            long off;  // element offset of (k0 + kk, e = 0) in the channel's operand
-            if (a.blocked) {  // consecutive threads: 8 spectra of one element, then the next
-                const int k8 = idx & 7;
-                e = (idx >> 3) & (XS_ST - 1);
-                kk = ((idx >> 9) << 3) + k8;
-                off = ((long)((k0 >> 3) + (idx >> 9)) * a.ne) * 8 + k8;
-            } else {  // consecutive threads: consecutive elements of one time sample
-                kk = idx / XS_ST;
-                e = idx - kk * XS_ST;
-                off = (long)(k0 + kk) * a.ld;
+        uint8_t *A = tileA(st), *B = tileB(st);
+        if (a.blocked) {
+            // XB[k/8][e][k%8]: every (8-sample block, element) is 64 contiguous bytes,
+            // copied as four 16-byte pairs; blocks past the input are zero-filled
+            for (int idx = tid; idx < (XS_KC / 8) * XS_ST * 4; idx += XS_THREADS) {
+                const int q = idx & 3, e = (idx >> 2) & (XS_ST - 1), sbl = idx >> 8;
+                const int kk = 8 * sbl + 2 * q;
+                const bool kin = k0 + 8 * sbl < a.nsp;
+                const long off = ((long)((k0 >> 3) + sbl) * a.ne) * 8 + 2 * q;
+                const int dst = xs_off(e, kk);
+                const bool ina = kin && e < nr;
+                cp_async16(A + dst, ina ? Xc + off + (long)(r0 + e) * 8 : Xc, ina ? 16 : 0);
+                if (has2) {  // the second channel's rows go to the B buffer
+                    cp_async16(B + dst, ina ? Xc2 + off + (long)(r0 + e) * 8 : Xc2, ina ? 16 : 0);
+                } else if (!diag) {
+                    const bool inb = kin && e < nq;
+                    cp_async16(B + dst, inb ? Xc + off + (long)(q0 + e) * 8 : Xc, inb ? 16 : 0);
+                }
             }
-            const int es = a.blocked ? 8 : 1;  // element stride
-            const bool kin = k0 + kk < a.nsp;
-            const bool ina = kin && e < nr;
-            float2 *da = A + kk * XS_RS + e;
-            cp_async8(da, ina ? Xc + off + (long)(r0 + e) * es : Xc, ina ? 8 : 0);
-            if (has2) {  // the second channel's rows go to the B buffer
-                cp_async8(B + kk * XS_RS + e, ina ? Xc2 + off + (long)(r0 + e) * es : Xc2,
-                          ina ? 8 : 0);
-            } else if (!diag) {
-                const bool inb = kin && e < nq;
-                cp_async8(B + kk * XS_RS + e, inb ? Xc + off + (long)(q0 + e) * es : Xc,
-                          inb ? 8 : 0);
+        } else {
+            // X[k*ld + e]: consecutive threads take consecutive elements of one sample
+            for (int idx = tid; idx < XS_KC * XS_ST; idx += XS_THREADS) {
+                const int kk = idx / XS_ST, e = idx - kk * XS_ST;
+                const long off = (long)(k0 + kk) * a.ld;
+                const bool kin = k0 + kk < a.nsp;
+                const int dst = xs_off(e, kk);
+                const bool ina = kin && e < nr;
+                cp_async8(A + dst, ina ? Xc + off + r0 + e : Xc, ina ? 8 : 0);
+                if (has2) {
+                    cp_async8(B + dst, ina ? Xc2 + off + r0 + e : Xc2, ina ? 8 : 0);
+                } else if (!diag) {
+                    const bool inb = kin && e < nq;
+                    cp_async8(B + dst, inb ? Xc + off + q0 + e : Xc, inb ? 8 : 0);
+                }
             }
         }
         cp_async_commit();
@@ -157,25 +183,34 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
         }
         __syncthreads();
         if (active) {
-            const float2 *A = cs ? tileB(st) : tileA(st);
-            const float2 *B = diag ? A : tileB(st);
-            for (int kk = ks; kk < XS_KC; kk += ksl) {
-                const float4 *pa = reinterpret_cast<const float4 *>(A + kk * XS_RS + mi * XS_MT);
-                const float4 *pb = reinterpret_cast<const float4 *>(B + kk * XS_RS + mj * XS_MT);
-                const float4 a01 = pa[0], a23 = pa[1], b01 = pb[0], b23 = pb[1];
-                const float2 av[4] = {make_float2(a01.x, a01.y), make_float2(a01.z, a01.w),
-                                      make_float2(a23.x, a23.y), make_float2(a23.z, a23.w)};
-                const float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w),
-                                      make_float2(b23.x, b23.y), make_float2(b23.z, b23.w)};
+            const uint8_t *A = cs ? tileB(st) : tileA(st);
+            const uint8_t *B = diag ? A : tileB(st);
+            for (int kp = ks; kp < XS_KC / 2; kp += ksl) {
+                // samples 2 kp and 2 kp + 1 of the micro-tile's 4 rows and 4 columns
+                float4 av[XS_MT], bv[XS_MT];
+#pragma unroll
+                for (int i = 0; i < XS_MT; i++) {
+                    av[i] = *reinterpret_cast<const float4 *>(A + xs_off(XS_MT * mi + i, 2 * kp));
+                    bv[i] = *reinterpret_cast<const float4 *>(B + xs_off(XS_MT * mj + i, 2 * kp));
+                }
 #pragma unroll
                 for (int i = 0; i < XS_MT; i++)
 #pragma unroll
                     for (int j = 0; j < XS_MT; j++) {
-                        // acc += a * conj(b)
+                        // acc += a * conj(b), sample 2 kp then 2 kp + 1
                         acc[i][j].x = fmaf(av[i].x, bv[j].x, acc[i][j].x);
                         acc[i][j].x = fmaf(av[i].y, bv[j].y, acc[i][j].x);
                         acc[i][j].y = fmaf(av[i].y, bv[j].x, acc[i][j].y);
                         acc[i][j].y = fmaf(-av[i].x, bv[j].y, acc[i][j].y);
+                    }
+#pragma unroll
+                for (int i = 0; i < XS_MT; i++)
+#pragma unroll
+                    for (int j = 0; j < XS_MT; j++) {
+                        acc[i][j].x = fmaf(av[i].z, bv[j].z, acc[i][j].x);
+                        acc[i][j].x = fmaf(av[i].w, bv[j].w, acc[i][j].x);
+                        acc[i][j].y = fmaf(av[i].w, bv[j].z, acc[i][j].y);
+                        acc[i][j].y = fmaf(-av[i].z, bv[j].w, acc[i][j].y);
                     }
             }
         }
