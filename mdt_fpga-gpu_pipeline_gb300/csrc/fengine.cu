@@ -17,6 +17,7 @@
 // `hist` (the PFB history carried between integrations, reference
 // MDT_OneStation_client.cu:1170) and the rest from `iq`.
 #include <cuda_bf16.h>
+#include <algorithm>
 #include <cuda_fp16.h>
 
 #include "fengine.cuh"
@@ -173,9 +174,11 @@ struct FengBCfg {
     static constexpr int MINB =
         (MDT_FENG16_SM_THREADS / THREADS) < 1 ? 1 : (MDT_FENG16_SM_THREADS / THREADS);
     static constexpr int RSTRIDE = fft::Shape<N>::PADN + 4;
-    // the transform's rows, then the block's int8 input rows (up to 8 + 7)
+    // the transform's rows, the block's int8 input rows (up to 8 + 7), then
+    // the FFT's compact twiddle table
     static constexpr size_t STAGE_OFF = (sizeof(float2) * (size_t)RSTRIDE * SB8 + 15) / 16 * 16;
-    static constexpr size_t SMEM = STAGE_OFF + (size_t)(SB8 + 7) * 2 * N;
+    static constexpr size_t TW_OFF = STAGE_OFF + (size_t)(SB8 + 7) * 2 * N;
+    static constexpr size_t SMEM = TW_OFF + sizeof(float2) * (size_t)fft::tw_compact_len<N>();
 };
 
 template <int CPI>
@@ -226,15 +229,12 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_b
                  : "memory");
 }
 
-// The block's input rows (spectra s0 .. s0+7+NT-1 of element e) are first
-// copied into shared memory `stage` with cp.async, all in flight at once
-// (rows past the input are zero-filled); the tap sum then reads them there.
+// The block's input rows (spectra s0 .. s0+7+NT-1 of element e) are copied
+// into shared memory `stage` with cp.async, all in flight at once (rows past
+// the input are zero-filled) and committed as one group.
 template <int N, int NT, int THREADS>
-__device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, int e, float2 *smem,
-                                                   int rstride, uint8_t *stage)
+__device__ __forceinline__ void stage_rows_async(const FengArgs &a, int s0, int e, uint8_t *stage)
 {
-    constexpr int CPI = (N / THREADS >= 2) ? 2 : 1;  // channels per thread item
-    constexpr int ITEMS = N / CPI;
     constexpr int NROW = SB8 + NT - 1;
     constexpr int RCHUNKS = 2 * N / 16;  // 16-byte chunks per input row
     const long rowlen = (long)a.ne * N;
@@ -251,10 +251,53 @@ __device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, in
                    in ? 16 : 0);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// Waits for the staged rows, then forms the block's 8 tap sums from them
+// into the transform rows (no barrier after the sums).
+template <int N, int NT, int THREADS>
+__device__ __forceinline__ void tapsum_from_stage(const FengArgs &a, int s0, float2 *smem, int rstride,
+                                                  const uint8_t *stage)
+{
+    constexpr int CPI = (N / THREADS >= 2) ? 2 : 1;  // channels per thread item
+    constexpr int ITEMS = N / CPI;
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     for (int it = threadIdx.x; it < ITEMS; it += THREADS) {
         const int c0 = it * CPI;
+        if constexpr (CPI == 2 && MDT_FFT_F32X2) {
+            // the two channels c0, c0 + 1 as one packed FP32 pair: one f32x2
+            // fma per (row, tap) and component, each lane rounded as fmaf
+            float2 w2[NT];
+#pragma unroll
+            for (int i = 0; i < NT; i++)
+                w2[i] = __ldg(reinterpret_cast<const float2 *>(a.win + (long)i * N + c0));
+            float2 ar[SB8], ai[SB8];
+#pragma unroll
+            for (int r = 0; r < SB8; r++) ar[r] = ai[r] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < SB8 + NT - 1; j++) {
+                Samples<2> x;
+                x.load_shared(stage + (size_t)j * 2 * N + 2 * c0);
+                const float2 xr = make_float2(x.re[0], x.re[1]), xi = make_float2(x.im[0], x.im[1]);
+#pragma unroll
+                for (int r = 0; r < SB8; r++) {
+                    const int i = j - r;
+                    if (i >= 0 && i < NT) {
+                        ar[r] = __ffma2_rn(w2[i], xr, ar[r]);
+                        ai[r] = __ffma2_rn(w2[i], xi, ai[r]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < SB8; r++) {
+                const bool live = s0 + r < a.nsp;
+                float2 *row = smem + (size_t)r * rstride + fft::pad(c0);  // pad(c0 + 1) = pad(c0) + 1
+                row[0] = live ? make_float2(ar[r].x, ai[r].x) : make_float2(0.f, 0.f);
+                row[1] = live ? make_float2(ar[r].y, ai[r].y) : make_float2(0.f, 0.f);
+            }
+            continue;
+        }
         float w[NT][CPI];
 #pragma unroll
         for (int i = 0; i < NT; i++)
@@ -292,6 +335,16 @@ __device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, in
     }
 }
 
+// Stage, then tap sum; `mid()` runs while the copies are in flight.
+template <int N, int NT, int THREADS, class Mid>
+__device__ __forceinline__ void pfb_block8_to_smem(const FengArgs &a, int s0, int e, float2 *smem,
+                                                   int rstride, uint8_t *stage, Mid &&mid)
+{
+    stage_rows_async<N, NT, THREADS>(a, s0, e, stage);
+    mid();
+    tapsum_from_stage<N, NT, THREADS>(a, s0, smem, rstride, stage);
+}
+
 // Block decode: blk = (kc * NE + e) * 4 + jsub, s0 = 32 kc + 8 jsub.
 struct Block8 {
     int jsub, e, kc, s0;
@@ -307,46 +360,116 @@ struct Block8 {
 };
 
 // Tap sum + FFT of the block's 8 rows; the spectra stay in shared memory
-// (row r at fsm + r*RSTRIDE, channel c at pad(c)).
+// (row r at fsm + r*RSTRIDE, channel c at pad(c)).  The FFT reads its
+// twiddles from the compact table at TW_OFF (one 8-byte shared load per
+// power instead of a scattered global load).
 template <int N, int NT>
 __device__ __forceinline__ void fengine_block8(const FengArgs &a, const Block8 &b, float2 *fsm)
 {
     using C = FengBCfg<N>;
-    if constexpr (NT > 0)
+    float2 *tws = reinterpret_cast<float2 *>(reinterpret_cast<uint8_t *>(fsm) + C::TW_OFF);
+    auto fill_tw = [&]() { fft::fill_tw_compact<N>(tws, a.tw, (int)threadIdx.x, C::THREADS); };
+    if constexpr (NT > 0) {
         pfb_block8_to_smem<N, NT, C::THREADS>(a, b.s0, b.e, fsm, C::RSTRIDE,
-                                              reinterpret_cast<uint8_t *>(fsm) + C::STAGE_OFF);
-    else
+                                              reinterpret_cast<uint8_t *>(fsm) + C::STAGE_OFF,
+                                              fill_tw);
+    } else {
+        fill_tw();
         pfb_rows_to_smem<N, SB8, C::THREADS, true>(a, b.s0, b.e, fsm, C::RSTRIDE);
+    }
     __syncthreads();
     const int lrow = threadIdx.x / C::TPR;
     const int t = threadIdx.x - lrow * C::TPR;
     auto none_load = [](int) { return make_float2(0.f, 0.f); };
     auto none_store = [](int, float2) {};
-    fft::transform_row<N, C::TPR, false, false>(fsm + (size_t)lrow * C::RSTRIDE, t, a.tw,
-                                                none_load, none_store);
+    fft::transform_row_tws<N, C::TPR, false, false>(fsm + (size_t)lrow * C::RSTRIDE, t, tws,
+                                                    none_load, none_store);
 }
 
 // FP32 output in the 8-spectrum blocked layout of the plan's FP32 path:
 //   XB[c][sb][e][8] complex64, sb = s/8 (ceil(Nsp/8) blocks, spectra past
 //   Nsp zero): per channel one contiguous 64-byte run per block.
-template <int N, int NT>
-__global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
-    fengine_c64b_kernel(FengArgs a, float2 *__restrict__ XB, int nsb)
+template <int N>
+__device__ __forceinline__ void store_c64b(const float2 *fsm, const Block8 &b, float2 *XB, int ne, int nsb)
 {
     using C = FengBCfg<N>;
-    extern __shared__ float2 fsm[];
-    const Block8 b(a.ne);
-    const int sb = b.kc * 4 + b.jsub;
-    if (sb >= nsb) return;  // whole block: the last 32-spectrum chunk may hold fewer groups
-    fengine_block8<N, NT>(a, b, fsm);
-    float2 *base = XB + ((size_t)sb * a.ne + b.e) * SB8;
-    const size_t cstride = (size_t)nsb * a.ne * SB8;
+    float2 *base = XB + ((size_t)(b.kc * 4 + b.jsub) * ne + b.e) * SB8;
+    const size_t cstride = (size_t)nsb * ne * SB8;
     for (int it = threadIdx.x; it < N * 4; it += C::THREADS) {
         const int c = it >> 2, q = it & 3;  // q: pair of spectra
         const float2 v0 = fsm[(size_t)(2 * q) * C::RSTRIDE + fft::pad(c)];
         const float2 v1 = fsm[(size_t)(2 * q + 1) * C::RSTRIDE + fft::pad(c)];
         *reinterpret_cast<float4 *>(base + (size_t)c * cstride + 2 * q) =
             make_float4(v0.x, v0.y, v1.x, v1.y);
+    }
+}
+
+// Work unit u decodes as blockIdx.x does in Block8; units whose 8-spectrum
+// block lies past the last one (the tail of the last 32-spectrum chunk) hold
+// no work.
+__device__ __forceinline__ int next_c64b_unit(int u, int step, int nunits, int ne, int nsb)
+{
+    while (u < nunits && Block8(ne, u).kc * 4 + Block8(ne, u).jsub >= nsb) u += step;
+    return u;
+}
+
+// Nch >= 1024 with NT = 4 or 8: persistent blocks (as many as fit on the GPU at once), each
+// looping over units u = blockIdx.x, blockIdx.x + gridDim.x, ...  A unit's
+// input rows are staged while the previous unit's FFT and stores run: the
+// staging buffer is free once the tap sum has read it, so the next unit's
+// copies are issued right after the tap-sum barrier.  The compact twiddle
+// table is filled once per block.
+// Otherwise one block per unit (smaller blocks already share an SM several
+// at a time; NT = 0, other tap counts, forms the tap sums from global memory).
+template <int N, int NT>
+constexpr bool c64b_persistent()
+{
+    return NT > 0 && N >= 1024;
+}
+
+template <int N, int NT>
+__global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
+    fengine_c64b_kernel(FengArgs a, float2 *__restrict__ XB, int nsb, int nunits)
+{
+    using C = FengBCfg<N>;
+    extern __shared__ float2 fsm[];
+    if constexpr (!c64b_persistent<N, NT>()) {
+        const Block8 b(a.ne);
+        if (b.kc * 4 + b.jsub >= nsb) return;
+        fengine_block8<N, NT>(a, b, fsm);
+        store_c64b<N>(fsm, b, XB, a.ne, nsb);
+    } else {
+        uint8_t *stage = reinterpret_cast<uint8_t *>(fsm) + C::STAGE_OFF;
+        float2 *tws = reinterpret_cast<float2 *>(reinterpret_cast<uint8_t *>(fsm) + C::TW_OFF);
+        const int step = (int)gridDim.x;
+        int u = next_c64b_unit((int)blockIdx.x, step, nunits, a.ne, nsb);
+        if (u >= nunits) return;
+        {
+            const Block8 b(a.ne, u);
+            stage_rows_async<N, NT, C::THREADS>(a, b.s0, b.e, stage);
+        }
+        fft::fill_tw_compact<N>(tws, a.tw, (int)threadIdx.x, C::THREADS);
+        const int lrow = threadIdx.x / C::TPR;
+        const int t = threadIdx.x - lrow * C::TPR;
+        auto none_load = [](int) { return make_float2(0.f, 0.f); };
+        auto none_store = [](int, float2) {};
+        while (true) {
+            const Block8 b(a.ne, u);
+            // waits for the staged rows; its barrier also orders the previous
+            // unit's stores (reads of the rows) before the new tap sums
+            tapsum_from_stage<N, NT, C::THREADS>(a, b.s0, fsm, C::RSTRIDE, stage);
+            __syncthreads();  // rows complete, staging buffer free
+            const int un = next_c64b_unit(u + step, step, nunits, a.ne, nsb);
+            if (un < nunits) {
+                const Block8 bn(a.ne, un);
+                stage_rows_async<N, NT, C::THREADS>(a, bn.s0, bn.e, stage);
+            }
+            fft::transform_row_tws<N, C::TPR, false, false>(fsm + (size_t)lrow * C::RSTRIDE, t, tws,
+                                                            none_load, none_store);
+            store_c64b<N>(fsm, b, XB, a.ne, nsb);
+            if (un >= nunits) break;
+            u = un;
+        }
     }
 }
 
@@ -570,9 +693,19 @@ struct FengBRun {
                                              (int)C::SMEM);
         if (e != cudaSuccess) return cuda_status(e, "fengine_c64b smem attribute");
         const long nkc = (nsb + 3) / 4;
-        long blocks = (long)a.ne * nkc * 4;
-        if (blocks > 0x7fffffffL) return invalid("fengine_c64b: grid too large");
-        fengine_c64b_kernel<N, NT><<<(unsigned)blocks, C::THREADS, C::SMEM, stream>>>(a, XB, nsb);
+        const long units = (long)a.ne * nkc * 4;
+        if (units > 0x7fffffffL) return invalid("fengine_c64b: grid too large");
+        long grid = units;
+        if (c64b_persistent<N, NT>()) {  // the blocks that fit on the GPU at once
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fengine_c64b_kernel<N, NT>,
+                                                              C::THREADS, C::SMEM);
+            if (e != cudaSuccess) return cuda_status(e, "fengine_c64b occupancy");
+            grid = std::min(units, (long)std::max(per_sm, 1) * sm_count());
+        }
+        if (grid == 0) return MDT_SUCCESS;
+        fengine_c64b_kernel<N, NT><<<(unsigned)grid, C::THREADS, C::SMEM, stream>>>(a, XB, nsb,
+                                                                                   (int)units);
         return launch_status("fengine_c64b_kernel");
     }
 };
