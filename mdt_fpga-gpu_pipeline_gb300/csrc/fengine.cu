@@ -167,6 +167,12 @@ __global__ void __launch_bounds__(FengCfg<N>::THREADS, FengCfg<N>::MINB) fengine
 
 constexpr int SB8 = 8;  // spectra per block
 
+// Tap sums of the spectrum-block kernels convert int8 samples with integer
+// and FP32 add instructions instead of the int-to-float conversion unit.
+#ifndef MDT_FENG_I2F_MAGIC
+#define MDT_FENG_I2F_MAGIC 1
+#endif
+
 template <int N>
 struct FengBCfg {
     static constexpr int TPR = feng_tpr(N, MDT_FENG16_TPR);
@@ -277,9 +283,25 @@ __device__ __forceinline__ void tapsum_from_stage(const FengArgs &a, int s0, flo
             for (int r = 0; r < SB8; r++) ar[r] = ai[r] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int j = 0; j < SB8 + NT - 1; j++) {
+#if MDT_FENG_I2F_MAGIC
+                // int8 -> float without the conversion unit: byte u = x + 128
+                // placed in the mantissa of 2^23 gives 2^23 + u exactly, and
+                // subtracting 2^23 + 128 leaves x exactly
+                const uint32_t wv =
+                    *reinterpret_cast<const uint32_t *>(stage + (size_t)j * 2 * N + 2 * c0) ^ 0x80808080u;
+                constexpr float kOff = -8388736.0f;  // -(2^23 + 128)
+                const float2 off = make_float2(kOff, kOff);
+                const float2 xr = __fadd2_rn(make_float2(__uint_as_float(__byte_perm(wv, 0x4B000000u, 0x7540)),
+                                                         __uint_as_float(__byte_perm(wv, 0x4B000000u, 0x7542))),
+                                             off);
+                const float2 xi = __fadd2_rn(make_float2(__uint_as_float(__byte_perm(wv, 0x4B000000u, 0x7541)),
+                                                         __uint_as_float(__byte_perm(wv, 0x4B000000u, 0x7543))),
+                                             off);
+#else
                 Samples<2> x;
                 x.load_shared(stage + (size_t)j * 2 * N + 2 * c0);
                 const float2 xr = make_float2(x.re[0], x.re[1]), xi = make_float2(x.im[0], x.im[1]);
+#endif
 #pragma unroll
                 for (int r = 0; r < SB8; r++) {
                     const int i = j - r;
