@@ -28,6 +28,10 @@ constexpr int XS_ST = 64;       // super-tile width
 constexpr int XS_MT = 4;        // micro-tile width
 constexpr int XS_KC = 32;       // time samples staged per chunk
 constexpr int XS_THREADS = 256;
+// Complex multiply-adds of the micro-tile as packed f32x2 fmas.
+#ifndef MDT_XS_F32X2
+#define MDT_XS_F32X2 1
+#endif
 // Staged operand rows are element-major: row e holds the chunk's XS_KC time
 // samples as XS_KC/2 16-byte pairs; pair j of row e sits at position
 // j ^ ((e / XS_MT) & 7), so the 16-byte loads of lanes with different
@@ -193,6 +197,30 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
                     av[i] = *reinterpret_cast<const float4 *>(A + xs_off(XS_MT * mi + i, 2 * kp));
                     bv[i] = *reinterpret_cast<const float4 *>(B + xs_off(XS_MT * mj + i, 2 * kp));
                 }
+#if MDT_XS_F32X2
+                // acc += a * conj(b) on (re, im) pairs, one f32x2 fma per term:
+                //   acc += (a.re, a.im) * (b.re, b.re);  acc += (a.im, -a.re) * (b.im, b.im)
+                // each lane the same fmaf sequence as the scalar form below
+#pragma unroll
+                for (int h = 0; h < 2; h++) {  // sample 2 kp, then 2 kp + 1
+                    float2 a1[XS_MT], a2[XS_MT];
+#pragma unroll
+                    for (int i = 0; i < XS_MT; i++) {
+                        const float ar = h ? av[i].z : av[i].x, ai = h ? av[i].w : av[i].y;
+                        a1[i] = make_float2(ar, ai);
+                        a2[i] = make_float2(ai, -ar);
+                    }
+#pragma unroll
+                    for (int j = 0; j < XS_MT; j++) {
+                        const float br = h ? bv[j].z : bv[j].x, bi = h ? bv[j].w : bv[j].y;
+#pragma unroll
+                        for (int i = 0; i < XS_MT; i++) {
+                            acc[i][j] = __ffma2_rn(a1[i], make_float2(br, br), acc[i][j]);
+                            acc[i][j] = __ffma2_rn(a2[i], make_float2(bi, bi), acc[i][j]);
+                        }
+                    }
+                }
+#else
 #pragma unroll
                 for (int i = 0; i < XS_MT; i++)
 #pragma unroll
@@ -212,6 +240,7 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
                         acc[i][j].y = fmaf(av[i].w, bv[j].z, acc[i][j].y);
                         acc[i][j].y = fmaf(-av[i].z, bv[j].w, acc[i][j].y);
                     }
+#endif
             }
         }
         __syncthreads();  // buffer st is overwritten by the next stage() call
