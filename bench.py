@@ -41,8 +41,8 @@ sys.path.insert(0, ROOT)
 # workload, from ncu captures of one c2 integration (profiles/fengine_c64b_c2.txt,
 # profiles/xengine_herm_f32_c2.txt); the per-launch work of the bench is the
 # same integration, so no scaling is needed.
-NCU_TRAFFIC = {"fengine_c64b": 672.424e6 + 2633.477e6,
-               "xengine_herm_f32": 2684.438e6 + 26.985e6}
+NCU_TRAFFIC = {"fengine_c64b": 677.995e6 + 2637.297e6,
+               "xengine_herm_f32": 2684.435e6 + 26.480e6}
 # The tensor path's kernels on one c3 integration (Nsp = 8192), scaled from ncu
 # captures at Nsp = 1024 (profiles/fengine_tc_c3.txt, profiles/xengine_tc_c3.txt):
 # the F-engine's reads and writes and the X-engine's operand reads grow with
