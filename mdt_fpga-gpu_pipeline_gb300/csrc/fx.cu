@@ -78,7 +78,8 @@ struct mdt_fx_plan_s {
     bool streaming = false;
     size_t bytes = 0;
     // host pipeline (mdt_fx_execute_host), allocated on first use
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host -> device input copies
+    cudaStream_t out_stream = nullptr;   // device -> host visibility copies
     int8_t *stage_in[2] = {nullptr, nullptr};
     float2 *stage_vis[2] = {nullptr, nullptr};
     cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr},
@@ -113,6 +114,7 @@ void release(mdt_fx_plan p)
         if (p->ev_out[i]) cudaEventDestroy(p->ev_out[i]);
     }
     if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
+    if (p->out_stream) cudaStreamDestroy(p->out_stream);
     for (cudaEvent_t e : p->tev) cudaEventDestroy(e);
     delete p;
 }
@@ -475,33 +477,56 @@ MDT_API mdt_status mdt_fx_stream_push(mdt_fx_plan plan, const int8_t *iq, void *
     return stream_push(plan, iq, vis);
 }
 
+// Creates what the host pipeline still lacks (a failed call leaves what it
+// made, and the next call completes it); ready when the last event exists.
 static mdt_status host_pipeline_init(mdt_fx_plan p)
 {
-    if (p->copy_stream) return MDT_SUCCESS;
+    if (p->ev_out[1]) return MDT_SUCCESS;
     const mdt_fx_desc &d = p->d;
     const size_t in_bytes = spectrum_bytes(d) * (size_t)(d.nspectra + d.ntaps - 1);
     const size_t vb = sizeof(float2) * (size_t)d.nchannels * d.nelements * d.nelements;
-    cudaError_t e = cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaSuccess;
+    if (!p->copy_stream) e = cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !p->out_stream)
+        e = cudaStreamCreateWithFlags(&p->out_stream, cudaStreamNonBlocking);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
-        e = cudaMalloc(&p->stage_in[i], in_bytes);
-        if (e == cudaSuccess) e = cudaMalloc(&p->stage_vis[i], vb);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_in[i], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_done[i], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_out[i], cudaEventDisableTiming);
+        if (!p->stage_in[i]) {
+            void *q = nullptr;
+            e = cudaMalloc(&q, in_bytes);
+            if (e == cudaSuccess) {
+                p->stage_in[i] = static_cast<int8_t *>(q);
+                p->bytes += in_bytes;
+            }
+        }
+        if (e == cudaSuccess && !p->stage_vis[i]) {
+            void *q = nullptr;
+            e = cudaMalloc(&q, vb);
+            if (e == cudaSuccess) {
+                p->stage_vis[i] = static_cast<float2 *>(q);
+                p->bytes += vb;
+            }
+        }
+        if (e == cudaSuccess && !p->ev_in[i])
+            e = cudaEventCreateWithFlags(&p->ev_in[i], cudaEventDisableTiming);
+        if (e == cudaSuccess && !p->ev_done[i])
+            e = cudaEventCreateWithFlags(&p->ev_done[i], cudaEventDisableTiming);
+        if (e == cudaSuccess && !p->ev_out[i])
+            e = cudaEventCreateWithFlags(&p->ev_out[i], cudaEventDisableTiming);
     }
     if (e != cudaSuccess) {
         mdt::cuda_status(e, "fx_execute_host: staging buffers");
         return MDT_ERR_ALLOC;
     }
-    p->bytes += 2 * (in_bytes + vb);
     return MDT_SUCCESS;
 }
 
 // Host-memory pipeline: integration j's samples are copied host->device on a
 // copy stream while integration j-1 is processed and j-2's visibilities are
-// copied back; the PFB history is carried on the device between integrations
-// (the reference's rank 1 -> rank 2 -> rank 3 chain, MDT_OneStation_client.cu
-// :1048, :1083-1128, :1170, :1199).  Returns after the last copy completes.
+// copied back on a third stream (so the input copies, which bound the
+// pipeline, run back to back); the PFB history is carried on the device
+// between integrations (the reference's rank 1 -> rank 2 -> rank 3 chain,
+// MDT_OneStation_client.cu :1048, :1083-1128, :1170, :1199).  Returns after
+// the last copy completes.
 MDT_API mdt_status mdt_fx_execute_host(mdt_fx_plan plan, const int8_t *h_iq, int nint,
                                        void *h_vis)
 {
@@ -517,14 +542,15 @@ MDT_API mdt_status mdt_fx_execute_host(mdt_fx_plan plan, const int8_t *h_iq, int
     const size_t sb = spectrum_bytes(d);
     const size_t vb = sizeof(float2) * (size_t)d.nchannels * d.nelements * d.nelements;
     const int nh = d.ntaps - 1;
-    cudaStream_t cs = plan->copy_stream, ks = plan->stream;
+    cudaStream_t cs = plan->copy_stream, os = plan->out_stream, ks = plan->stream;
     plan->streaming = false;
     plan->cur = 0;
     auto cuda = [&](cudaError_t e, const char *w) { return mdt::cuda_status(e, w); };
-    // the copy stream starts after everything already queued on the compute stream
+    // the copy streams start after everything already queued on the compute stream
     cudaEvent_t start = plan->ev_out[1];
     if ((st = cuda(cudaEventRecord(start, ks), "record")) != MDT_SUCCESS) return st;
     if ((st = cuda(cudaStreamWaitEvent(cs, start, 0), "wait")) != MDT_SUCCESS) return st;
+    if ((st = cuda(cudaStreamWaitEvent(os, start, 0), "wait")) != MDT_SUCCESS) return st;
     auto upload = [&](int j) -> mdt_status {
         const int b = j & 1;
         const size_t off = (j == 0) ? 0 : ((size_t)j * d.nspectra + nh) * sb;
@@ -550,14 +576,15 @@ MDT_API mdt_status mdt_fx_execute_host(mdt_fx_plan plan, const int8_t *h_iq, int
         if ((st = stream_push(plan, plan->stage_in[b], plan->stage_vis[b])) != MDT_SUCCESS)
             return st;
         if ((st = cuda(cudaEventRecord(plan->ev_done[b], ks), "record")) != MDT_SUCCESS) return st;
-        if ((st = cuda(cudaStreamWaitEvent(cs, plan->ev_done[b], 0), "wait")) != MDT_SUCCESS)
+        if ((st = cuda(cudaStreamWaitEvent(os, plan->ev_done[b], 0), "wait")) != MDT_SUCCESS)
             return st;
         if ((st = cuda(cudaMemcpyAsync((char *)h_vis + (size_t)j * vb, plan->stage_vis[b], vb,
-                                       cudaMemcpyDeviceToHost, cs), "D2H")) != MDT_SUCCESS)
+                                       cudaMemcpyDeviceToHost, os), "D2H")) != MDT_SUCCESS)
             return st;
-        if ((st = cuda(cudaEventRecord(plan->ev_out[b], cs), "record")) != MDT_SUCCESS) return st;
+        if ((st = cuda(cudaEventRecord(plan->ev_out[b], os), "record")) != MDT_SUCCESS) return st;
     }
-    return cuda(cudaStreamSynchronize(cs), "fx_execute_host: sync");
+    if ((st = cuda(cudaStreamSynchronize(cs), "fx_execute_host: sync")) != MDT_SUCCESS) return st;
+    return cuda(cudaStreamSynchronize(os), "fx_execute_host: sync");
 }
 
 MDT_API mdt_status mdt_fx_set_timing(mdt_fx_plan plan, int enable)

@@ -119,7 +119,8 @@ def test_fused_fengine_bit_identical_to_dropin_chain(mdt, cuda):
 
 
 @pytest.mark.parametrize("ne,nch,ntaps,nsp,nint", [(8, 256, 8, 64, 4), (3, 32, 8, 2, 5),
-                                                   (5, 64, 4, 3, 3)])
+                                                   (5, 64, 4, 3, 3), (4, 1024, 8, 40, 3),
+                                                   (3, 2048, 4, 17, 2)])
 def test_streaming_history_vs_oracle(mdt, cuda, oracle, ne, nch, ntaps, nsp, nint):
     cfg = mdt.configs.small(mdt.configs.C2, nelements=ne, nchannels=nch, ntaps=ntaps,
                             nspectra=nsp, nint=nint)
@@ -146,6 +147,29 @@ def test_streaming_history_vs_oracle(mdt, cuda, oracle, ne, nch, ntaps, nsp, nin
         seg = iqh[j * nsp * sb:(j * nsp + nsp + ntaps - 1) * sb]
         ref = oracle.fx(seg, winh, ne, nch, ntaps, nsp)
         assert rel_fro(vis_stream[j].cpu().numpy(), ref) < TOL_FP32
+    plan.close()
+
+
+@pytest.mark.parametrize("ne,nch,ntaps,nsp,nint", [(6, 1024, 8, 48, 5), (3, 64, 4, 5, 1)])
+def test_execute_host_matches_device_run(mdt, cuda, ne, nch, ntaps, nsp, nint):
+    """The host-buffer pipeline (input copies, compute and visibility copies on
+    three streams, staging buffers reused from the third integration on)
+    returns the device run's visibilities bit for bit, also when called twice."""
+    cfg = mdt.configs.small(mdt.configs.C2, nelements=ne, nchannels=nch, ntaps=ntaps,
+                            nspectra=nsp, nint=nint)
+    total = nint * nsp + ntaps - 1
+    iq = gen_iq(mdt, cfg, 0, total)
+    win = window(mdt, nch, ntaps)
+    plan = mdt.FxPlan(ne, nch, ntaps, nsp)
+    plan.set_window(win)
+    vis_dev = torch.empty(nint, nch, ne, ne, dtype=torch.complex64, device="cuda")
+    plan.execute(iq, nint, vis_dev)
+    torch.cuda.synchronize()
+    h_iq = iq.cpu().pin_memory()
+    for _ in range(2):
+        h_vis = torch.full((nint, nch, ne, ne), float("nan"), dtype=torch.complex64).pin_memory()
+        plan.execute_host(h_iq, nint, h_vis)
+        assert torch.equal(h_vis.view(torch.int64), vis_dev.cpu().view(torch.int64))
     plan.close()
 
 
