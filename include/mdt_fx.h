@@ -144,8 +144,8 @@ MDT_API mdt_status mdt_fengine_f32(int ne, int nch, int ntaps, int nsp, const in
                                    const float *window, void *X, cudaStream_t stream);
 
 /* Fused F-engine, FP32, into the 8-spectrum blocked layout the plan's FP32
- * path uses:  XB[c][s/8][e][s%8] complex64 (ceil(Nsp/8) blocks, spectra past
- * Nsp zero) -- per channel one 64-byte run per (8 spectra, element).  Same
+ * path uses:  XB[s/8][c][e][s%8] complex64 (ceil(Nsp/8) blocks, spectra past
+ * Nsp zero) -- one 64-byte run per (8 spectra, channel, element).  Same
  * values as mdt_fengine_f32 (bit-identical), Nch <= 2048. */
 MDT_API mdt_status mdt_fengine_c64b(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
                                     const float *window, void *XB, cudaStream_t stream);

@@ -408,15 +408,15 @@ __device__ __forceinline__ void fengine_block8(const FengArgs &a, const Block8 &
                                                     none_load, none_store);
 }
 
-// FP32 output in the 8-spectrum blocked layout of the plan's FP32 path:
-//   XB[c][sb][e][8] complex64, sb = s/8 (ceil(Nsp/8) blocks, spectra past
-//   Nsp zero): per channel one contiguous 64-byte run per block.
+// FP32 output in the 8-spectrum blocked layout of the plan's FP32 path (XB,
+// fengine.cuh): one 64-byte run per channel for the block's (8 spectra,
+// element).
 template <int N>
 __device__ __forceinline__ void store_c64b(const float2 *fsm, const Block8 &b, float2 *XB, int ne, int nsb)
 {
     using C = FengBCfg<N>;
-    float2 *base = XB + ((size_t)(b.kc * 4 + b.jsub) * ne + b.e) * SB8;
-    const size_t cstride = (size_t)nsb * ne * SB8;
+    float2 *base = XB + (size_t)(b.kc * 4 + b.jsub) * xb_block_stride(ne, N, nsb) + (size_t)b.e * SB8;
+    const size_t cstride = (size_t)xb_chan_stride(ne, N, nsb);
     for (int it = threadIdx.x; it < N * 4; it += C::THREADS) {
         const int c = it >> 2, q = it & 3;  // q: pair of spectra
         const float2 v0 = fsm[(size_t)(2 * q) * C::RSTRIDE + fft::pad(c)];
@@ -614,15 +614,19 @@ __global__ void __launch_bounds__(FengBCfg<N>::THREADS, FengBCfg<N>::MINB)
 }
 
 // Per-channel mean power over the elements and spectra of an XB buffer
-// (nsb blocks of 8 spectra, nsp valid): pw[c] = mean |X|^2.
+// (nsb blocks of 8 spectra, nsp valid): pw[c] = mean |X|^2.  Each thread sums
+// its values in (block, element, spectrum) order whatever the layout's
+// strides, so the result does not depend on them.
 __global__ void channel_power_kernel(const float2 *__restrict__ XB, int ne, int nsb, int nsp,
-                                     float *__restrict__ pw)
+                                     long cstride, long bstride, float *__restrict__ pw)
 {
     const int c = blockIdx.x;
-    const float2 *xc = XB + (size_t)c * nsb * ne * 8;
+    const float2 *xc = XB + (size_t)c * cstride;
+    const int run = ne * 8;  // complex64 values of one (block, channel)
     double acc = 0.0;
-    for (long i = threadIdx.x; i < (long)nsb * ne * 8; i += blockDim.x) {
-        const float2 v = xc[i];
+    for (long i = threadIdx.x; i < (long)nsb * run; i += blockDim.x) {
+        const long sb = i / run;
+        const float2 v = xc[sb * bstride + (i - sb * run)];
         acc += (double)v.x * v.x + (double)v.y * v.y;
     }
     __shared__ double red[256];
@@ -804,7 +808,9 @@ mdt_status fengine_x16_batched(int nch, int ntaps, const FJob *jobs, int njobs, 
 mdt_status channel_scales(const float2 *XB, int ne, int nch, int nsp, float target_rms, float *pw,
                           float *scales, cudaStream_t stream)
 {
-    channel_power_kernel<<<nch, 256, 0, stream>>>(XB, ne, (nsp + 7) / 8, nsp, pw);
+    const long nsb = (nsp + 7) / 8;
+    channel_power_kernel<<<nch, 256, 0, stream>>>(XB, ne, (int)nsb, nsp, xb_chan_stride(ne, nch, nsb),
+                                                  xb_block_stride(ne, nch, nsb), pw);
     mdt_status st = launch_status("channel_power_kernel");
     if (st != MDT_SUCCESS) return st;
     scales_from_power_kernel<<<(unsigned)cdiv(nch, 256), 256, 0, stream>>>(pw, nch, target_rms,
@@ -827,7 +833,7 @@ mdt_status fengine_q8(int ne, int nch, int ntaps, int nsp, const int8_t *hist, i
     return dispatch_block8(nch, ntaps, run);
 }
 
-// FP32 F-engine into the 8-spectrum blocked layout XB (fengine_c64b_kernel).
+// FP32 F-engine into the 8-spectrum blocked layout XB (fengine.cuh).
 mdt_status fengine_c64b(int ne, int nch, int ntaps, int nsp, const int8_t *hist, int nhist,
                         const int8_t *iq, const float *win, float2 *XB, cudaStream_t stream)
 {

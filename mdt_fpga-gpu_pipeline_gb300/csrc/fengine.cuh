@@ -31,6 +31,24 @@ mdt_status fengine_x16_batched(int nch, int ntaps, const FJob *jobs, int njobs, 
 // total work items.
 mdt_status fengine_tc_batched(int ntaps, const FJob *jobs, int njobs, long nwork, int *err,
                               cudaStream_t stream);
+// The FP32 path's F-output XB: complex64 in blocks of 8 spectra (ceil(Nsp/8)
+// blocks, spectra past Nsp zero); every (block, channel, element) is one
+// 64-byte run of the block's 8 spectra.  Block-major, XB[s/8][c][e][s%8], so an
+// F-engine unit's runs for all its channels lie within one block's Nch*NE*64
+// bytes (MDT_XB_BLOCK_MAJOR 0: channel-major XB[c][s/8][e][s%8]).
+#ifndef MDT_XB_BLOCK_MAJOR
+#define MDT_XB_BLOCK_MAJOR 1
+#endif
+// complex64 elements between consecutive channels / consecutive 8-spectrum blocks
+__host__ __device__ inline long xb_chan_stride(int ne, int nch, long nsb)
+{
+    return MDT_XB_BLOCK_MAJOR ? (long)ne * 8 : nsb * ne * 8;
+}
+__host__ __device__ inline long xb_block_stride(int ne, int nch, long nsb)
+{
+    return MDT_XB_BLOCK_MAJOR ? (long)nch * ne * 8 : (long)ne * 8;
+}
+
 mdt_status check_dims(int ne, int nch, int ntaps, int nsp);
 const float2 *fft_twiddles(int n, mdt_status *st);
 

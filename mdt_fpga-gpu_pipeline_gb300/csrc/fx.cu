@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "fengine.cuh"
 #include "mdt_common.cuh"
 
 namespace mdt {
@@ -144,7 +145,7 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
     }
     mdt_status st;
     if (d.precision == MDT_PREC_FP32) {
-        // F-output in the 8-spectrum blocked layout XB[c][s/8][e][s%8]
+        // F-output in the 8-spectrum blocked layout XB (fengine.cuh)
         const long nsb = (d.nspectra + 7) / 8;
         if (d.nchannels <= 2048)
             st = mdt::fengine_c64b(d.nelements, d.nchannels, d.ntaps, d.nspectra, hist, nhist, iq,
@@ -166,8 +167,10 @@ mdt_status one_integration(mdt_fx_plan p, const int8_t *hist, int nhist, const i
         } else {
             if (st != MDT_SUCCESS) return st;
             if (t1) cudaEventRecord(t1, p->stream);
-            st = mdt::xengine_herm_f32(d.nelements, d.nchannels, d.nspectra, p->X, nullptr, 0,
-                                       nsb * 8 * d.nelements, (float2 *)vis, nullptr,
+            st = mdt::xengine_herm_f32(d.nelements, d.nchannels, d.nspectra, p->X, nullptr,
+                                       mdt::xb_block_stride(d.nelements, d.nchannels, nsb),
+                                       mdt::xb_chan_stride(d.nelements, d.nchannels, nsb),
+                                       (float2 *)vis, nullptr,
                                        d.nelements, (long)d.nelements * d.nelements,
                                        make_float2(1.0f / d.nspectra, 0.f), make_float2(0.f, 0.f),
                                        true, p->stream, 1);

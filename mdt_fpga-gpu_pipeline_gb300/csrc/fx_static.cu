@@ -24,6 +24,7 @@
 #include <mutex>
 #include <vector>
 
+#include "fengine.cuh"
 #include "mdt_common.cuh"
 
 namespace mdt {
@@ -112,7 +113,8 @@ extern "C" MDT_API mdt_status mdt_fx_integrate_static(int ne, int nch, int ntaps
                                           d->twiddles, stream);
     if (st != MDT_SUCCESS) return st;
     const long nsb = (nsp + 7) / 8;
-    return mdt::xengine_herm_f32(ne, nch, nsp, d->scratch, nullptr, 0, nsb * 8 * ne,
+    return mdt::xengine_herm_f32(ne, nch, nsp, d->scratch, nullptr, mdt::xb_block_stride(ne, nch, nsb),
+                                 mdt::xb_chan_stride(ne, nch, nsb),
                                  (float2 *)vis, nullptr, ne, (long)ne * ne,
                                  make_float2(1.0f / nsp, 0.f), make_float2(0.f, 0.f), true,
                                  stream, 1);

@@ -48,7 +48,7 @@ struct XengArgs {
     long ldv, vstride;
     float2 alpha, beta;
     int beta_zero;
-    int blocked;  // operand layout: 0 = X[k*ld + e]; 1 = XB[k/8][e][k%8] (NE rows per block)
+    int blocked;  // operand layout: 0 = X[k*ld + e]; 1 = blocks of 8 samples, X[(k/8)*ld + e*8 + k%8]
     int dual;     // NE <= 64: a block takes two channels (A and B buffers hold one each)
     long nbatch;
 };
@@ -132,13 +132,14 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     auto stage = [&](int k0, int st) {
         uint8_t *A = tileA(st), *B = tileB(st);
         if (a.blocked) {
-            // XB[k/8][e][k%8]: every (8-sample block, element) is 64 contiguous bytes,
-            // copied as four 16-byte pairs; blocks past the input are zero-filled
+            // blocks of 8 samples ld apart: every (8-sample block, element) is 64
+            // contiguous bytes, copied as four 16-byte pairs; blocks past the input
+            // are zero-filled
             for (int idx = tid; idx < (XS_KC / 8) * XS_ST * 4; idx += XS_THREADS) {
                 const int q = idx & 3, e = (idx >> 2) & (XS_ST - 1), sbl = idx >> 8;
                 const int kk = 8 * sbl + 2 * q;
                 const bool kin = k0 + 8 * sbl < a.nsp;
-                const long off = ((long)((k0 >> 3) + sbl) * a.ne) * 8 + 2 * q;
+                const long off = (long)((k0 >> 3) + sbl) * a.ld + 2 * q;
                 const int dst = xs_off(e, kk);
                 const bool ina = kin && e < nr;
                 cp_async16(A + dst, ina ? Xc + off + (long)(r0 + e) * 8 : Xc, ina ? 16 : 0);
@@ -320,7 +321,7 @@ mdt_status xengine_herm_f32(int ne, long nbatch, int nsp, const float2 *X,
     a.npairs = a.nsuper * (a.nsuper + 1) / 2;
     a.X = X;
     a.Xptrs = Xptrs;
-    a.ld = ld;
+    a.ld = (blocked && ld == 0) ? (long)ne * 8 : ld;  // blocked: complex64 between 8-sample blocks
     a.xstride = xstride;
     a.V = V;
     a.Vptrs = Vptrs;

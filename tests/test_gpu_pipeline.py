@@ -253,7 +253,7 @@ def test_blocked_fengine_matches_reference_layout(mdt, cuda, ne, nch, ntaps, nsp
     XB = torch.full((nch * nsb * ne * 8,), float("nan"), dtype=torch.complex64, device="cuda")
     mdt.fengine_c64b(ne, nch, ntaps, nsp, iq, win, XB)
     torch.cuda.synchronize()
-    xb = XB.view(nch, nsb, ne, 8).permute(0, 1, 3, 2).reshape(nch, nsb * 8, ne)
+    xb = XB.view(nsb, nch, ne, 8).permute(1, 0, 3, 2).reshape(nch, nsb * 8, ne)
     assert torch.all(xb[:, nsp:, :] == 0)
     ref = X.view(nch, nsp, ne)
     assert torch.equal(xb[:, :nsp, :].contiguous().view(torch.int64), ref.view(torch.int64))
