@@ -287,6 +287,8 @@ def fengine_f32(ne, nch, ntaps, nsp, iq, window, X, stream=None):
 
 
 def fengine_c64b(ne, nch, ntaps, nsp, iq, window, XB, stream=None):
+    """FP32 F-engine into XB[s/8][c][e][s%8] complex64 (ceil(nsp/8) blocks of 8
+    spectra, spectra past nsp zero), bit-identical to fengine_f32."""
     check(lib().mdt_fengine_c64b(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(XB),
                                  stream_handle(stream)), "fengine_c64b")
 
