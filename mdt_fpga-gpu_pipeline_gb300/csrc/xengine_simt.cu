@@ -131,6 +131,8 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
     // stage chunk k0 into buffer st: 64 element rows of XS_KC samples per operand
     auto stage = [&](int k0, int st) {
         uint8_t *A = tileA(st), *B = tileB(st);
+        // rows the micro-tiles read: rows past the operand's last element up to
+        // the micro-tile edge are zero-filled, rows beyond it are not staged
         if (a.blocked) {
             // blocks of 8 samples ld apart: every (8-sample block, element) is 64
             // contiguous bytes, copied as four 16-byte pairs; blocks past the input
@@ -142,10 +144,12 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
                 const long off = (long)((k0 >> 3) + sbl) * a.ld + 2 * q;
                 const int dst = xs_off(e, kk);
                 const bool ina = kin && e < nr;
-                cp_async16(A + dst, ina ? Xc + off + (long)(r0 + e) * 8 : Xc, ina ? 16 : 0);
-                if (has2) {  // the second channel's rows go to the B buffer
-                    cp_async16(B + dst, ina ? Xc2 + off + (long)(r0 + e) * 8 : Xc2, ina ? 16 : 0);
-                } else if (!diag) {
+                if (e < ((nr + XS_MT - 1) & ~(XS_MT - 1))) {
+                    cp_async16(A + dst, ina ? Xc + off + (long)(r0 + e) * 8 : Xc, ina ? 16 : 0);
+                    if (has2)  // the second channel's rows go to the B buffer
+                        cp_async16(B + dst, ina ? Xc2 + off + (long)(r0 + e) * 8 : Xc2, ina ? 16 : 0);
+                }
+                if (!has2 && !diag && e < ((nq + XS_MT - 1) & ~(XS_MT - 1))) {
                     const bool inb = kin && e < nq;
                     cp_async16(B + dst, inb ? Xc + off + (long)(q0 + e) * 8 : Xc, inb ? 16 : 0);
                 }
@@ -158,10 +162,11 @@ __global__ void __launch_bounds__(XS_THREADS, 3) xengine_herm_f32_kernel(XengArg
                 const bool kin = k0 + kk < a.nsp;
                 const int dst = xs_off(e, kk);
                 const bool ina = kin && e < nr;
-                cp_async8(A + dst, ina ? Xc + off + r0 + e : Xc, ina ? 8 : 0);
-                if (has2) {
-                    cp_async8(B + dst, ina ? Xc2 + off + r0 + e : Xc2, ina ? 8 : 0);
-                } else if (!diag) {
+                if (e < ((nr + XS_MT - 1) & ~(XS_MT - 1))) {
+                    cp_async8(A + dst, ina ? Xc + off + r0 + e : Xc, ina ? 8 : 0);
+                    if (has2) cp_async8(B + dst, ina ? Xc2 + off + r0 + e : Xc2, ina ? 8 : 0);
+                }
+                if (!has2 && !diag && e < ((nq + XS_MT - 1) & ~(XS_MT - 1))) {
                     const bool inb = kin && e < nq;
                     cp_async8(B + dst, inb ? Xc + off + q0 + e : Xc, inb ? 8 : 0);
                 }
