@@ -30,7 +30,7 @@
  *   Ntaps   = PFB taps (4..128); Nsp = spectra per integration (2..16384)
  *   int8 I/Q input    iq[(s*NE + e)*Nch + c][2]  (I then Q), the reference's
  *                     Spectrum -> Element -> Channel order
- *                     (MDT_device_functions.cu:172-174)
+ *                     (MDT_device_functions.cu:124-126)
  *   window            W[i*Nch + c], float, tap-major
  *   F-engine output   X[(c*Nsp + s)*NE + e], complex64 (ReorderFOutput layout)
  *   visibilities      V[c][q*NE + r] = (1/Nsp) sum_s X[c][s][r] conj(X[c][s][q]),
@@ -86,20 +86,20 @@ MDT_API const char *mdt_last_error(void);
  *    launches them).  Each returns MDT_ERR_CUDA if the launch fails.
  * ---------------------------------------------------------------------- */
 
-/* PFB_Window_min4term_BH (reference MDT_device_functions.cu:100-136):
+/* PFB_Window_min4term_BH (reference MDT_device_functions.cu:52-88):
  * W[n] = sinc((n - Ntaps*Nch/2)/Nch) * minimum 4-term Blackman-Harris. */
 MDT_API mdt_status mdt_launch_PFB_Window_min4term_BH(unsigned gx, unsigned gy, unsigned gz, unsigned bx,
     unsigned by, unsigned bz, cudaStream_t stream,
                                                      int nchannels, int ntaps, float *window);
 
-/* PpS_Batch (reference MDT_device_functions.cu:161-209), bit-exact:
+/* PpS_Batch (reference MDT_device_functions.cu:113-161), bit-exact:
  * NE = gz, Nsp = gy; input (Nsp+Ntaps-1) spectra of complex64. */
 MDT_API mdt_status mdt_launch_PpS_Batch(unsigned gx, unsigned gy, unsigned gz, unsigned bx,
     unsigned by, unsigned bz, cudaStream_t stream, int nchannels,
                                         int ntaps, float *window, void *insignal,
                                         void *polystruct);
 
-/* ReorderFOutput (reference MDT_device_functions.cu:231-256), bit-exact:
+/* ReorderFOutput (reference MDT_device_functions.cu:183-208), bit-exact:
  * Nsp = gz; any block shape (the reference needs block (32,32)). */
 MDT_API mdt_status mdt_launch_ReorderFOutput(unsigned gx, unsigned gy, unsigned gz, unsigned bx,
     unsigned by, unsigned bz, cudaStream_t stream,
@@ -108,7 +108,7 @@ MDT_API mdt_status mdt_launch_ReorderFOutput(unsigned gx, unsigned gy, unsigned 
 
 /* Hamming windowed sinc of the benchmark configurations (no reference
  * counterpart; the reference's window is an input array to PpS_Batch,
- * MDT_device_functions.cu:163):
+ * MDT_device_functions.cu:113-117):
  *   W[n] = sinc((n - Ntaps*Nch/2)/Nch) * (0.54 - 0.46 cos(2 pi n/(Ntaps*Nch))). */
 MDT_API mdt_status mdt_window_hamming_sinc(int nchannels, int ntaps, float *window,
                                            cudaStream_t stream);
@@ -530,10 +530,17 @@ MDT_API mdt_status mdt_pfb_tap_grad(int ne, int nch, int ntaps, int nsp, const v
  * (MDT_STATIC_SCRATCH_BYTES at build time) that every GPU loading the
  * library holds until exit: requests needing more than that --
  * Nch * ceil(Nsp/8)*8 * NE * 8 bytes -- or Nch > 2048 return
- * MDT_ERR_INVALID_VALUE.  The first call on a device (with that device
- * current) looks up the arrays' device addresses and uploads the FFT
- * twiddle tables, so make it before any stream capture.  All calls on a
- * device share the scratch; calls whose GPU work overlaps race on it.
+ * MDT_ERR_INVALID_VALUE, as do the shapes every entry point rejects (Nch
+ * not a power of two in [32, 16384], NE, Ntaps or Nsp out of range).  The
+ * first call on a device (with that device current) looks up the arrays'
+ * device addresses and uploads the FFT twiddle tables, so make it before
+ * any stream capture.  Under CUDA's default lazy module loading that first
+ * call is also when the 96 MiB are committed on the device (at context
+ * creation with CUDA_MODULE_LOADING=EAGER): a real-time caller makes one
+ * warm-up call per device outside its loop.  All calls on a device share
+ * the scratch, which keeps the last call's contents (every call overwrites
+ * the part it reads, so nothing needs clearing); calls whose GPU work
+ * overlaps race on it.
  * Calls no cudaMalloc/cudaFree. */
 MDT_API mdt_status mdt_fx_integrate_static(int ne, int nch, int ntaps, int nsp, const int8_t *iq,
                                            const float *window, void *vis, cudaStream_t stream);

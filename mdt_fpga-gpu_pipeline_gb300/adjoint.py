@@ -122,25 +122,30 @@ def gain_error(est, true):
 
 
 def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9, step=0.5,
-                true_gains=None, callback=None):
+                true_gains=None, callback=None, g0=None):
     """Per-antenna, per-channel complex gains by gradient descent.
 
-    Loss  L(g) = sum_c sum_{a<b} |V(g)_ab - data_ab|^2  with V(g) the FX
-    correlation of `iq` under gains g (FxCorrelate; since V(g)_ab =
-    g_a conj(g_b) model_ab, this is the loss |data - g_a g_b^* model|^2 against
-    the source model `model` = V(1)).  Gradients come from the adjoint
-    kernels; each step is preconditioned per (channel, antenna) by the
-    diagonal of the Gauss-Newton normal equations,
+    Loss  L(g) = sum_c sum_{a<b} |data_ab - V(g)_ab|^2,  V(g) = the FX
+    correlation of the model's samples `iq` under gains g (FxCorrelate).  With
+    `iq` the noise-free streams of the sky model's sources (known flux and
+    delays) and model = V(1) their correlation, V(g)_ab = g_a conj(g_b) model_ab,
+    so this is the loss |data - g_a g_b^* model|^2 of a calibration against
+    the source model, with `data` the measured (gained, noisy) visibilities.
+    Gradients come from the adjoint kernels; each step is preconditioned per
+    (channel, antenna) by the diagonal of the Gauss-Newton normal equations,
         h_ca = sum_{b != a} |g_cb|^2 |model_c,ab|^2,
     computed with the iterate in FP64 on the GPU:  g <- g - step * grad / (2h).
-    Stops when the relative loss drops below `tol` (or after `iters` steps).
-    Returns (gains complex64 [Nch, NE], history list of (loss, error or None))."""
+    Starts from `g0` (default unit gains); stops when the relative loss
+    change between steps drops below `tol`, or the relative loss itself does
+    (or after `iters` steps).  Returns (gains complex64 [Nch, NE], history
+    list of (relative loss, error against true_gains or None))."""
     dev = iq.device
     mask = baseline_mask(ne, dev)
     mr = torch.view_as_real(model.detach().to(torch.complex64).contiguous()).double()
     m2 = mr[..., 0] ** 2 + mr[..., 1] ** 2  # |model|^2, [c, q, r]
     m2 = m2 * (1 - torch.eye(ne, dtype=torch.float64, device=dev))
-    g = torch.ones(nch, ne, dtype=torch.complex128, device=dev)
+    g = (torch.ones(nch, ne, dtype=torch.complex128, device=dev) if g0 is None
+         else g0.detach().to(torch.complex128).clone())
     data = data.detach()
     dnorm = float(_sqnorm(data[:, mask]))
     hist = []
@@ -153,9 +158,52 @@ def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9,
         hist.append((float(loss.detach()) / dnorm, err))
         if callback is not None:
             callback(len(hist), hist[-1])
-        if hist[-1][0] < tol:
+        if hist[-1][0] < tol or (len(hist) > 1 and
+                                 abs(hist[-2][0] - hist[-1][0]) <= tol * hist[-1][0]):
             break
         gg = g.real ** 2 + g.imag ** 2
         h = (m2 * gg[:, None, :]).sum(dim=2)  # model is Hermitian: |M_ab| = |M_ba|
         g = g - step * gv.grad.to(torch.complex128) / (2 * h)
     return g.to(torch.complex64), hist
+
+
+def c5_calibration_inputs(mdt, cfg, taps, model_scale=4, seed_salt=9):
+    """The inputs of a configuration-5 gain calibration on the current device.
+
+    data : visibilities of the configured sky (the sources plus unit receiver
+           noise at the configured SNR, int8 I/Q from the integer generator)
+           through the F-engine with true gains applied to its output,
+           Y = diag(g) X  (FxCorrelate), multiplied by model_scale^2;
+    iq_model : the same sources alone (known flux, delays from the element
+           positions; no receiver noise), generated at model_scale times
+           their amplitude so that int8 rounding stays ~2e-4 of their power,
+           and the model's visibilities model = V(1) of those streams;
+    g_true : gains with amplitude U[0.8, 1.2] and phase U[-pi, pi] per
+           (channel, element), seeded.
+    data and model share the source streams (the generator is keyed by
+    source and time), never the noise.  Returns (data, iq_model, model,
+    g_true)."""
+    dev = taps.device
+    ne, nch, ntaps, nsp = cfg.nelements, cfg.nchannels, cfg.ntaps, cfg.nspectra
+    total = nsp + ntaps - 1
+    ssig, sdel = cfg.sources()
+
+    def t(a):
+        return torch.from_numpy(a).to(dev)
+
+    iq = torch.empty(total * ne * nch * 2, dtype=torch.int8, device=dev)
+    B.synth_iq(cfg.seed, ne, nch, 0, total, t(cfg.sigma_q8()), iq,
+               src_sigma_q8=t(ssig), src_delay=t(sdel))
+    iq_model = torch.empty_like(iq)
+    B.synth_iq(cfg.seed, ne, nch, 0, total, t(0 * cfg.sigma_q8()), iq_model,
+               src_sigma_q8=t(ssig * model_scale), src_delay=t(sdel))
+    import numpy as np
+    rng = np.random.default_rng([cfg.seed, seed_salt])
+    g_true = t((rng.uniform(0.8, 1.2, (nch, ne)) *
+                np.exp(1j * rng.uniform(-np.pi, np.pi, (nch, ne)))).astype(np.complex64))
+    ones = torch.ones(nch, ne, dtype=torch.complex64, device=dev)
+    with torch.no_grad():
+        data = fx_correlate(iq, taps, g_true, ne, nch, ntaps, nsp) * float(model_scale ** 2)
+        model = fx_correlate(iq_model, taps, ones, ne, nch, ntaps, nsp)
+    del iq
+    return data, iq_model, model, g_true

@@ -11,8 +11,8 @@
 //    kernels take them);
 //  * ReorderFOutput stages full 32x32 tiles with whatever block shape it is
 //    given; the reference loads only blockDim.x channels of each tile
-//    (:241-245) and writes 32, which is wrong for its documented NE < 32
-//    geometry (:223).
+//    (:193,197) and writes 32, which is wrong for its documented NE < 32
+//    geometry (:175).
 #include <math.h>
 #include <mutex>
 #include <stdio.h>
@@ -65,7 +65,7 @@ int sm_count()
 // kernels are part of the library's interface, so their stubs are exported.
 #define MDT_KERNEL_EXPORT __attribute__((visibility("default")))
 
-// Minimum 4-term Blackman-Harris windowed sinc (reference :100-136), with the
+// Minimum 4-term Blackman-Harris windowed sinc (reference :52-88), with the
 // reference's float argument conventions; sinpif/cospif are CUDA's.
 __global__ MDT_KERNEL_EXPORT void PFB_Window_min4term_BH(int Nchannels, int Ntaps, float *Window)
 {
@@ -81,7 +81,7 @@ __global__ MDT_KERNEL_EXPORT void PFB_Window_min4term_BH(int Nchannels, int Ntap
     }
 }
 
-// Polyphase structure (reference :161-209):
+// Polyphase structure (reference :113-161):
 //   out[s][e][c] = sum_{i<Ntaps} W[i*Nch + c] * in[s+i][e][c]
 // accumulated with fmaf in increasing i from zero (bit-exact with the
 // reference).  NE = gridDim.z, spectrum s = blockIdx.y, element e = blockIdx.z.
@@ -109,7 +109,7 @@ __global__ MDT_KERNEL_EXPORT void PpS_Batch(int Nchannels, int Ntaps, float *Win
     }
 }
 
-// Corner turn (reference :231-256):  X[(c*Nsp + s)*NE + e] = F[(s*NE + e)*Nch + c]
+// Corner turn (reference :183-208):  X[(c*Nsp + s)*NE + e] = F[(s*NE + e)*Nch + c]
 // with Nsp = gridDim.z and s = blockIdx.z.  32x32 tiles through shared memory
 // (33-column rows), tiles walked grid-stride over (blockIdx.x -> elements,
 // blockIdx.y -> channels), every tile fully staged whatever the block shape.

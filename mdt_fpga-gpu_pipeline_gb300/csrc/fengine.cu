@@ -6,12 +6,12 @@
 // A block transforms ROWS rows (spectrum s, elements e0..e0+ROWS-1):
 //  * the tap sum P[c] = sum_i W[i*Nch + c] * iq[s+i][e][c] is formed with
 //    16-byte vector loads into shared memory, accumulated with fmaf from zero
-//    in increasing i, the order of PpS_Batch (MDT_device_functions.cu:191-200),
+//    in increasing i, the order of PpS_Batch (MDT_device_functions.cu:143-152),
 //    so P is bit-identical to the drop-in kernel's output on the same samples;
 //  * the FFT passes run in shared memory (fft_core.cuh), the last one leaves
 //    the spectrum in natural order in shared memory;
 //  * the block writes X[(c*Nsp + s)*NE + e] (ReorderFOutput's layout,
-//    MDT_device_functions.cu:255): for each channel the ROWS elements are
+//    MDT_device_functions.cu:207): for each channel the ROWS elements are
 //    contiguous.
 // Input spectra may come from two buffers: the first `nhist` spectra from
 // `hist` (the PFB history carried between integrations, reference

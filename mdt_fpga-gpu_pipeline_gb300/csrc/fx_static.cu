@@ -16,7 +16,11 @@
 // the first call on each device, with that device current, looks their
 // device addresses up with cudaGetSymbolAddress and fills the twiddle tables
 // (a host-to-device copy); that first call should therefore come before any
-// stream capture.  Every call on a device shares the same scratch and
+// stream capture.  Under CUDA's default lazy module loading the device
+// memory of the arrays is committed when this file's module is first used,
+// that is, by the first call on each device (with CUDA_MODULE_LOADING=EAGER,
+// when the context is created).  A real-time caller therefore makes one
+// warm-up call per device outside its loop.  Every call on a device shares the same scratch and
 // overwrites all of the part it uses before reading it, so nothing needs
 // clearing between calls; calls whose work overlaps on the GPU (different
 // streams, or the same array used from two threads) race on the scratch.
@@ -58,8 +62,11 @@ std::vector<DeviceSlots> g_slots;
 
 // Once per device, with the device current: device addresses of the two
 // arrays and the twiddle tables exp(-2 pi i k / N) (double, rounded to float,
-// the same values as the library's per-device tables).
-mdt_status setup_current_device(DeviceSlots **out)
+// the same values as the library's per-device tables).  The two addresses
+// are copied out while the lock is held: a first call on a higher device
+// index grows g_slots and may move its elements, so no reference into the
+// table outlives the lock.
+mdt_status setup_current_device(float2 **scratch, float2 **twiddles)
 {
     int dev = 0;
     mdt_status st = mdt::cuda_status(cudaGetDevice(&dev), "fx_integrate_static: device");
@@ -68,10 +75,11 @@ mdt_status setup_current_device(DeviceSlots **out)
     if ((int)g_slots.size() <= dev) g_slots.resize(dev + 1);
     DeviceSlots &d = g_slots[dev];
     if (!d.ready) {
-        st = mdt::cuda_status(cudaGetSymbolAddress((void **)&d.scratch, g_fx_scratch),
+        float2 *sp = nullptr, *tp = nullptr;
+        st = mdt::cuda_status(cudaGetSymbolAddress((void **)&sp, g_fx_scratch),
                               "fx_integrate_static: scratch address");
         if (st != MDT_SUCCESS) return st;
-        st = mdt::cuda_status(cudaGetSymbolAddress((void **)&d.twiddles, g_fx_twiddles),
+        st = mdt::cuda_status(cudaGetSymbolAddress((void **)&tp, g_fx_twiddles),
                               "fx_integrate_static: twiddle address");
         if (st != MDT_SUCCESS) return st;
         std::vector<float2> h(kTwiddleEntries);
@@ -80,13 +88,16 @@ mdt_status setup_current_device(DeviceSlots **out)
                 double a = -2.0 * 3.141592653589793238462643383279502884 * (double)k / (double)n;
                 h[n - 32 + k] = make_float2((float)cos(a), (float)sin(a));
             }
-        st = mdt::cuda_status(cudaMemcpy(d.twiddles, h.data(), sizeof(float2) * h.size(),
+        st = mdt::cuda_status(cudaMemcpy(tp, h.data(), sizeof(float2) * h.size(),
                                          cudaMemcpyHostToDevice),
                               "fx_integrate_static: twiddle upload");
         if (st != MDT_SUCCESS) return st;
+        d.scratch = sp;
+        d.twiddles = tp;
         d.ready = true;
     }
-    *out = &d;
+    *scratch = d.scratch;
+    *twiddles = d.twiddles;
     return MDT_SUCCESS;
 }
 
@@ -106,14 +117,14 @@ extern "C" MDT_API mdt_status mdt_fx_integrate_static(int ne, int nch, int ntaps
                             std::to_string(need) + " bytes (Nch * ceil(Nsp/8)*8 * NE * 8), more "
                             "than the static scratch of " + std::to_string(kScratchBytes) +
                             " bytes");
-    DeviceSlots *d = nullptr;
-    st = setup_current_device(&d);
+    float2 *scratch = nullptr, *twiddles = nullptr;
+    st = setup_current_device(&scratch, &twiddles);
     if (st != MDT_SUCCESS) return st;
-    st = mdt::fengine_c64b_given_twiddles(ne, nch, ntaps, nsp, iq, window, d->scratch,
-                                          d->twiddles, stream);
+    st = mdt::fengine_c64b_given_twiddles(ne, nch, ntaps, nsp, iq, window, scratch, twiddles,
+                                          stream);
     if (st != MDT_SUCCESS) return st;
     const long nsb = (nsp + 7) / 8;
-    return mdt::xengine_herm_f32(ne, nch, nsp, d->scratch, nullptr, mdt::xb_block_stride(ne, nch, nsb),
+    return mdt::xengine_herm_f32(ne, nch, nsp, scratch, nullptr, mdt::xb_block_stride(ne, nch, nsb),
                                  mdt::xb_chan_stride(ne, nch, nsb),
                                  (float2 *)vis, nullptr, ne, (long)ne * ne,
                                  make_float2(1.0f / nsp, 0.f), make_float2(0.f, 0.f), true,

@@ -11,7 +11,7 @@
  * the reference calls (closed libraries, no golden vectors in the reference);
  * they are pinned against numpy's FFT and einsum and a naive DFT.
  *
- * Build: cc -O2 -fopenmp -ffp-contract=off -shared -fPIC (oracle/build.py).
+ * Build: cc -O3 -fopenmp -ffp-contract=off -shared -fPIC (oracle/oracle.py).
  * -ffp-contract=off keeps every a*b+c as a rounded multiply and a rounded
  * add, except where fmaf() is written explicitly (PpS_Batch's own order).
  */
@@ -41,7 +41,7 @@
 /* Minimum 4-term Blackman-Harris windowed sinc, evaluated in double:
  *   W[n] = sinc((n - Ntaps*Nch/2)/Nch) * (0.35875 - 0.48829 cos(2 pi n/L)
  *          + 0.14128 cos(4 pi n/L) - 0.01168 cos(6 pi n/L)),  L = Ntaps*Nch
- * following PFB_Window_min4term_BH, MDT_device_functions.cu:100-136
+ * following PFB_Window_min4term_BH, MDT_device_functions.cu:52-88
  * (argument conventions kept: sinc centre at L/2, cos argument 2n/L in
  * units of pi). */
 void mdt_oracle_window_bh4(int nch, int ntaps, double *w)
@@ -74,7 +74,7 @@ void mdt_oracle_window_hamming_sinc(int nch, int ntaps, float *w)
 
 /* ------------------------------------------------- bit-exact restatements */
 
-/* PpS_Batch (MDT_device_functions.cu:161-209) in float with the kernel's own
+/* PpS_Batch (MDT_device_functions.cu:113-161) in float with the kernel's own
  * operation order: per output, tmp = 0; for i in 0..Ntaps-1:
  *   tmp.x = fmaf(W[i*Nch+c], In[s+i][e][c].x, tmp.x)   (likewise .y)
  * Input spectra s+i, output spectrum s, element stride Nch, spectrum stride
@@ -99,7 +99,7 @@ void mdt_oracle_pps_f32_exact(int nch, int ntaps, int ne, int nsp, const float *
     }
 }
 
-/* ReorderFOutput (MDT_device_functions.cu:231-256) index map, moving 8-byte
+/* ReorderFOutput (MDT_device_functions.cu:183-208) index map, moving 8-byte
  * complex values:  X[(c*Nsp + s)*NE + e] = F[(s*NE + e)*Nch + c]. */
 void mdt_oracle_reorder_c64(int ne, int nch, int nsp, const uint64_t *F, uint64_t *X)
 {

@@ -8,15 +8,15 @@
  * TEST INFRASTRUCTURE ONLY: nothing in the product library links or calls this.
  *
  * The stages follow the reference sequence (MDT_OneStation_client.cu:1083-1128):
- *   PpS_Batch (MDT_device_functions.cu:161-209)   -> pps()
+ *   PpS_Batch (MDT_device_functions.cu:113-161)   -> pps()
  *   cufftExecC2C forward, unnormalised (:1105)    -> fft_rows()
- *   ReorderFOutput (MDT_device_functions.cu:231)  -> folded into the X stage
+ *   ReorderFOutput (MDT_device_functions.cu:183)  -> folded into the X stage
  *   cublasCgemmBatched(N, C, alpha=1/Nspectra)    -> xengine()
  *     (MDT_OneStation_client.cu:1128, alpha at :683-686)
  *
  * Layouts (all complex values interleaved re,im):
  *   input  int8 I/Q  in[(s*NE + e)*Nch + c][2],  s in [0, Nsp+Ntaps-1)
- *   window float     W[i*Nch + c]  (tap-major, MDT_device_functions.cu:195)
+ *   window float     W[i*Nch + c]  (tap-major, MDT_device_functions.cu:147)
  *   visibilities     V[k][q*NE + r] = alpha * sum_s X_c[s][r] * conj(X_c[s][q])
  *                    (column-major NE x NE per selected channel k, the cuBLAS
  *                    C-matrix layout with ldc=NE, MDT_OneStation_client.cu:1128)
@@ -96,9 +96,14 @@ int FN(mdt_oracle_fft_rows)(long rows, int n, REAL *data)
  *   nsel, sel : channel list (sel == NULL -> all nch channels, nsel ignored)
  *   V    : out, nsel x ne x ne complex REAL, column-major per channel,
  *          scaled by 1/nsp (cublas alpha, MDT_OneStation_client.cu:683)
- * Spectra are processed in blocks per OpenMP thread with private partial
- * visibility sums that are added in a fixed order at the end, so the result
- * does not depend on the thread count beyond that final, ordered reduction. */
+ * The reference's order, in chunks of spectra: the F-engine rows (PFB tap
+ * sum, FFT) of every (spectrum, element) of the chunk, the selected channels
+ * kept channel-major (the ReorderFOutput layout restricted to them); then the
+ * per-channel products, each visibility summed over the spectra in increasing
+ * order whatever the thread count (deterministic).  Only the lower triangle
+ * r >= q is summed: the upper one is its conjugate, which is what the full
+ * square gives bit for bit (the two products of a pair are the same
+ * roundings with the imaginary part negated). */
 int FN(mdt_oracle_fx)(int ne, int nch, int ntaps, int nsp, const int8_t *in,
                       const float *win, int nsel, const int *sel, REAL *V)
 {
@@ -118,72 +123,87 @@ int FN(mdt_oracle_fx)(int ne, int nch, int ntaps, int nsp, const int8_t *in,
     }
     REAL *tw = FN(make_twiddles)(nch);
     const size_t vlen = (size_t)nsel * ne * ne * 2;
-    const int nblk = 64; /* fixed spectrum blocking: result independent of threads */
-    REAL *partial = (REAL *)calloc((size_t)nblk * vlen, sizeof(REAL));
+    memset(V, 0, sizeof(REAL) * vlen);
     const size_t row = (size_t)nch * 2;
+    const size_t per_s = (size_t)nsel * ne * 2; /* REALs of selected F-output per spectrum */
+    long chunk = (long)(((size_t)1 << 25) / per_s);
+    if (chunk < 1) chunk = 1;
+    if (chunk > nsp) chunk = nsp;
+    REAL *xs = (REAL *)malloc(sizeof(REAL) * per_s * (size_t)chunk);
+    const int qb = 16; /* columns per product task */
+    const int nqb = (ne + qb - 1) / qb;
 
-    #pragma omp parallel
-    {
-        REAL *frow = (REAL *)malloc(sizeof(REAL) * row * (size_t)ne);
-        REAL *xsel = (REAL *)malloc(sizeof(REAL) * 2 * (size_t)ne * nsel);
-        #pragma omp for schedule(dynamic, 1)
-        for (int b = 0; b < nblk; b++) {
-            int s0 = (int)((long)nsp * b / nblk), s1 = (int)((long)nsp * (b + 1) / nblk);
-            REAL *acc = partial + (size_t)b * vlen;
-            for (int s = s0; s < s1; s++) {
-                for (int e = 0; e < ne; e++) {
-                    REAL *x = frow + row * e;
-                    /* polyphase sum, tap i applied to spectrum s+i
-                     * (MDT_device_functions.cu:191-200) */
-                    for (int c = 0; c < nch; c++) {
-                        REAL re = 0, im = 0;
-                        for (int i = 0; i < ntaps; i++) {
-                            const int8_t *p = in + 2 * (((size_t)(s + i) * ne + e) * nch + c);
-                            REAL w = (REAL)win[(size_t)i * nch + c];
-                            re += w * (REAL)p[0];
-                            im += w * (REAL)p[1];
-                        }
-                        x[2 * c] = re; x[2 * c + 1] = im;
+    for (long s0 = 0; s0 < nsp; s0 += chunk) {
+        const long ns = (nsp - s0 < chunk) ? nsp - s0 : chunk;
+        #pragma omp parallel
+        {
+            REAL *x = (REAL *)malloc(sizeof(REAL) * row);
+            #pragma omp for schedule(static)
+            for (long rr = 0; rr < ns * ne; rr++) {
+                const long t = rr / ne, s = s0 + t;
+                const int e = (int)(rr % ne);
+                /* polyphase sum, tap i applied to spectrum s+i
+                 * (MDT_device_functions.cu:143-152) */
+                for (int c = 0; c < nch; c++) {
+                    REAL re = 0, im = 0;
+                    for (int i = 0; i < ntaps; i++) {
+                        const int8_t *p = in + 2 * (((size_t)(s + i) * ne + e) * nch + c);
+                        REAL w = (REAL)win[(size_t)i * nch + c];
+                        re += w * (REAL)p[0];
+                        im += w * (REAL)p[1];
                     }
-                    FN(fft_row)(nch, logn, x, tw);
-                    for (int k = 0; k < nsel; k++) {
-                        xsel[2 * ((size_t)k * ne + e)] = x[2 * chan[k]];
-                        xsel[2 * ((size_t)k * ne + e) + 1] = x[2 * chan[k] + 1];
-                    }
+                    x[2 * c] = re; x[2 * c + 1] = im;
                 }
-                /* V_c[r + q*ne] += X[r] * conj(X[q]) (cublas OP_N x OP_C) */
+                FN(fft_row)(nch, logn, x, tw);
                 for (int k = 0; k < nsel; k++) {
-                    const REAL *xk = xsel + 2 * (size_t)k * ne;
-                    REAL *vk = acc + 2 * (size_t)k * ne * ne;
-                    for (int q = 0; q < ne; q++) {
-                        REAL qr = xk[2 * q], qi = xk[2 * q + 1];
-                        REAL *vq = vk + 2 * (size_t)q * ne;
-                        for (int r = 0; r < ne; r++) {
-                            REAL rr = xk[2 * r], ri = xk[2 * r + 1];
-                            vq[2 * r] += rr * qr + ri * qi;
-                            vq[2 * r + 1] += ri * qr - rr * qi;
-                        }
+                    REAL *d = xs + 2 * (((size_t)k * ns + t) * ne + e);
+                    d[0] = x[2 * chan[k]];
+                    d[1] = x[2 * chan[k] + 1];
+                }
+            }
+            free(x);
+        }
+        /* V_c[r + q*ne] += X[r] * conj(X[q]) (cublas OP_N x OP_C), r >= q */
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (long task = 0; task < (long)nsel * nqb; task++) {
+            const int k = (int)(task / nqb), q0 = (int)(task % nqb) * qb;
+            const int q1 = (q0 + qb < ne) ? q0 + qb : ne;
+            REAL *vk = V + 2 * (size_t)k * ne * ne;
+            for (long t = 0; t < ns; t++) {
+                const REAL *xk = xs + 2 * ((size_t)k * ns + t) * ne;
+                for (int q = q0; q < q1; q++) {
+                    const REAL qr = xk[2 * q], qi = xk[2 * q + 1];
+                    REAL *vq = vk + 2 * (size_t)q * ne;
+                    for (int r = q; r < ne; r++) {
+                        const REAL rr = xk[2 * r], ri = xk[2 * r + 1];
+                        vq[2 * r] += rr * qr + ri * qi;
+                        vq[2 * r + 1] += ri * qr - rr * qi;
                     }
                 }
             }
         }
-        free(frow);
-        free(xsel);
     }
-    REAL scale = (REAL)1 / (REAL)nsp;
-    for (size_t j = 0; j < vlen; j++) {
-        REAL sum = 0;
-        for (int b = 0; b < nblk; b++) sum += partial[(size_t)b * vlen + j];
-        V[j] = sum * scale;
+    const REAL scale = (REAL)1 / (REAL)nsp;
+    #pragma omp parallel for schedule(static)
+    for (long k = 0; k < nsel; k++) {
+        REAL *vk = V + 2 * (size_t)k * ne * ne;
+        for (int q = 0; q < ne; q++)
+            for (int r = q; r < ne; r++) {
+                REAL *lo = vk + 2 * ((size_t)q * ne + r), *up = vk + 2 * ((size_t)r * ne + q);
+                lo[0] *= scale;
+                lo[1] *= scale;
+                up[0] = lo[0];
+                up[1] = -lo[1];
+            }
     }
-    free(partial);
+    free(xs);
     free(tw);
     free(chan);
     return 0;
 }
 
 /* X-engine alone on a channel-major complex input X[c][s][e] (the
- * ReorderFOutput output layout, MDT_device_functions.cu:255):
+ * ReorderFOutput output layout, MDT_device_functions.cu:207):
  * V[c][q*ne + r] = alpha * sum_s X[c][s][r] conj(X[c][s][q]). */
 void FN(mdt_oracle_xengine)(int ne, int nch, int nsp, const REAL *X, REAL alpha, REAL *V)
 {

@@ -5,7 +5,8 @@ the smoke check in __graft_entry__ and the CPU-baseline leg of bench.py; the
 product library never uses it.
 
 build() compiles the C restatement into oracle/_build/libmdt_oracle.so with
-gcc/cc (-fopenmp, -ffp-contract=off).  Every function takes numpy arrays and
+gcc/cc (-O3 -fopenmp -ffp-contract=off; without -ffast-math no sum is
+reassociated, so vectorisation does not change a result).  Every function takes numpy arrays and
 returns numpy arrays; complex arrays are numpy complex64/complex128.
 """
 import ctypes
@@ -30,7 +31,7 @@ def build(force=False):
             return _LIB_PATH
     cc = os.environ.get("CC", "gcc")
     tmp = _LIB_PATH + ".tmp%d" % os.getpid()
-    cmd = [cc, "-O2", "-fopenmp", "-ffp-contract=off", "-shared", "-fPIC", "-std=c11",
+    cmd = [cc, "-O3", "-fopenmp", "-ffp-contract=off", "-shared", "-fPIC", "-std=c11",
            _SRC[0], "-o", tmp, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, _LIB_PATH)

@@ -5,7 +5,7 @@ The reference ships no tests, fixtures or known-answer vectors. Its kernels
 (PFB_Window_min4term_BH, PpS_Batch, ReorderFOutput in
 MDT_OneStation_client/MDT_device_functions.cu) are compiled for the CPU by
 oracle/build_ref.sh and run here, block by block, with the launch geometry
-the reference documents (MDT_device_functions.cu:92-98, 153-159, 223-228;
+the reference documents (MDT_device_functions.cu:44-49, 105-110, 175-180;
 ReorderFOutput always with block (32,32), the geometry under which the
 reference kernel is correct). The outputs are stored with their seeded
 inputs in ref_kernels.npz.

@@ -1,0 +1,37 @@
+"""The harness that runs the reference's own GPU sequence (baseline/refseq.cu)
+builds here and exports its C entry points; the recipe that compiles the
+reference kernels skips cleanly when no reference checkout is named.  (It is
+a comparison arm: the library itself links neither cuFFT nor cuBLAS.)"""
+import os
+import subprocess
+
+from conftest import ROOT
+
+
+def test_refseq_harness_builds_and_exports():
+    from baseline import refseq
+    lib = refseq.build()
+    syms = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True,
+                          text=True).stdout
+    for name in ("refseq_create", "refseq_destroy", "refseq_set_input", "refseq_stage",
+                 "refseq_run", "refseq_read", "refseq_ptr", "refseq_window_bh",
+                 "refseq_last_error"):
+        assert name in syms, name
+    deps = subprocess.run(["readelf", "-d", lib], capture_output=True, text=True).stdout
+    assert "libcufft" in deps and "libcublas" in deps
+
+
+def test_reference_gpu_recipe_skips_without_checkout():
+    env = dict(os.environ)
+    env.pop("MDT_REFERENCE_DIR", None)
+    r = subprocess.run(["bash", os.path.join(ROOT, "baseline", "build_ref_gpu.sh")],
+                       capture_output=True, text=True, env=env)
+    assert r.returncode == 0 and "skipping" in r.stderr
+
+
+def test_library_links_no_cufft_or_cublas():
+    import importlib
+    mdt = importlib.import_module("mdt_fpga-gpu_pipeline_gb300")
+    lib = mdt.build()
+    deps = subprocess.run(["readelf", "-d", lib], capture_output=True, text=True).stdout
+    assert "cufft" not in deps and "cublas" not in deps

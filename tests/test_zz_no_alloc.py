@@ -3,11 +3,20 @@ memory, for callers that cannot allocate (a real-time ingest loop that must
 not take cudaMalloc's device synchronisation, a plugin host with a fixed
 device-memory budget, a foreign runtime that owns all allocations).  Its
 F-engine output and FFT twiddles live in the library's file-scope device
-arrays.  Called through the C ABI with ctypes, twice in a row with different
-shapes (the second call reuses the scratch the first one left behind), and
-checked against the plan entry point mdt_fx_execute within the FP32 path's
-tolerance.  This file is collected last so that a stop at its first failure
-leaves every other test already run."""
+arrays.
+
+Called through the C ABI with ctypes, several times in a row with different
+shapes (each call reuses the scratch the previous one left behind):
+  * free device memory is the same before and after the calls that follow
+    the first one (the first call on a device loads the module holding the
+    arrays);
+  * the output equals the plan entry point mdt_fx_execute bit for bit (both
+    run the same F-engine and X-engine with the same twiddle values);
+  * the output is within the FP32 path's 1e-5 of the FP64 oracle;
+  * shapes the entry point cannot serve are rejected with
+    MDT_ERR_INVALID_VALUE and a message.
+This file is collected last so that a stop at its first failure leaves every
+other test already run."""
 import ctypes
 
 import numpy as np
@@ -18,7 +27,7 @@ from conftest import rel_fro
 
 pytestmark = pytest.mark.gpu
 
-TOL_FP32 = 1e-5  # the FP32 path's tolerance (vs FP64 and between FP32 entry points)
+TOL_FP32 = 1e-5  # the FP32 path's tolerance against the FP64 oracle
 MDT_ERR_INVALID_VALUE = 1
 
 
@@ -39,38 +48,67 @@ def _inputs(mdt, cfg):
                  tone_q16=None if tone is None else torch.from_numpy(tone).cuda())
     win = torch.empty(nch * ntaps, dtype=torch.float32, device="cuda")
     mdt.window_hamming_sinc(nch, ntaps, win)
-    return iq, win
+    vis = torch.full((nch, ne, ne), float("nan"), dtype=torch.complex64, device="cuda")
+    return iq, win, vis
 
 
-def test_integrate_static_matches_plan_two_calls(mdt, cuda):
+def _call(mdt, f, cfg, iq, win, vis):
+    rc = f(cfg.nelements, cfg.nchannels, cfg.ntaps, cfg.nspectra, iq.data_ptr(),
+           win.data_ptr(), vis.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, mdt.lib().mdt_last_error()
+
+
+def test_integrate_static_matches_plan_and_oracle(mdt, oracle, cuda):
     f = _entry(mdt)
-    stream = torch.cuda.current_stream().cuda_stream
     cases = [mdt.configs.C1,  # NE=10, Nch=1024, Ntaps=4, Nsp=1000: 82 MB of scratch
              mdt.configs.small(mdt.configs.C2, nspectra=120, nint=1)]  # NE=40, Nch=2048, Ntaps=8
-    for cfg in cases:
+    bufs = [_inputs(mdt, cfg) for cfg in cases]
+    torch.cuda.synchronize()
+    # first call on this device: loads the module holding the static arrays
+    _call(mdt, f, cases[0], *bufs[0])
+    torch.cuda.synchronize()
+    first = bufs[0][2].clone()
+    free0, _ = torch.cuda.mem_get_info()
+    # then two more calls in a row, the second shape and the first again
+    for cfg, b in ((cases[1], bufs[1]), (cases[0], bufs[0])):
+        b[2].fill_(float("nan"))
+        _call(mdt, f, cfg, *b)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, "device memory changed across calls: %d -> %d" % (free0, free1)
+    assert torch.equal(first.view(torch.int64), bufs[0][2].view(torch.int64)), \
+        "repeated call on reused scratch differs"
+
+    for cfg, (iq, win, vis) in zip(cases, bufs):
         ne, nch, ntaps, nsp = cfg.nelements, cfg.nchannels, cfg.ntaps, cfg.nspectra
-        iq, win = _inputs(mdt, cfg)
-        vis = torch.full((nch, ne, ne), float("nan"), dtype=torch.complex64, device="cuda")
-        rc = f(ne, nch, ntaps, nsp, iq.data_ptr(), win.data_ptr(), vis.data_ptr(), stream)
-        assert rc == 0, mdt.lib().mdt_last_error()
         plan = mdt.FxPlan(ne, nch, ntaps, nsp)
         plan.set_window(win)
         ref = torch.full_like(vis, float("nan"))
         plan.execute(iq, 1, ref)
         torch.cuda.synchronize()
         plan.close()
-        v, r = vis.cpu().numpy(), ref.cpu().numpy()
+        v = vis.cpu().numpy()
         assert np.all(np.isfinite(v))
-        assert rel_fro(v, r.astype(np.complex128)) < TOL_FP32, cfg.name
+        assert np.array_equal(v.view(np.int64), ref.cpu().numpy().view(np.int64)), \
+            "%s: static entry point differs from mdt_fx_execute" % cfg.name
+        chans = np.array([0, 137 % nch, nch // 2, nch - 1], np.int32)
+        o = oracle.fx(iq.cpu().numpy(), win.cpu().numpy(), ne, nch, ntaps, nsp, channels=chans)
+        err = rel_fro(v[chans], o)
+        assert err < TOL_FP32, "%s: %.3e vs FP64" % (cfg.name, err)
 
 
-def test_integrate_static_rejects_oversized_request(mdt, cuda):
+@pytest.mark.parametrize("shape,why", [
+    ((256, 1024, 8, 1024), b"static scratch"),  # 2 GiB of F-output
+    ((16, 4096, 4, 64), b"Nch must be <= 2048"),
+    ((16, 1000, 4, 64), b"power of two"),
+])
+def test_integrate_static_rejects_unservable_shapes(mdt, cuda, shape, why):
     f = _entry(mdt)
-    ne, nch, ntaps, nsp = 256, 1024, 8, 1024  # 2 GiB of F-output: beyond the scratch
+    ne, nch, ntaps, nsp = shape
     iq = torch.zeros((nsp + ntaps - 1) * ne * nch * 2, dtype=torch.int8, device="cuda")
     win = torch.zeros(nch * ntaps, dtype=torch.float32, device="cuda")
     vis = torch.zeros(nch * ne * ne, dtype=torch.complex64, device="cuda")
     rc = f(ne, nch, ntaps, nsp, iq.data_ptr(), win.data_ptr(), vis.data_ptr(),
            torch.cuda.current_stream().cuda_stream)
     assert rc == MDT_ERR_INVALID_VALUE
-    assert b"static scratch" in mdt.lib().mdt_last_error()
+    assert why in mdt.lib().mdt_last_error()
