@@ -18,8 +18,17 @@
 // The reference's input is complex64 (int32 samples x 2^-19, :896-907); this
 // harness converts the same int8 I/Q the library reads to complex64 exactly.
 //
+// cuFFT and cuBLAS are opened with dlopen(RTLD_LOCAL | RTLD_DEEPBIND) and
+// their entry points taken with dlsym from those handles: libmdtfx.so exports
+// the same names (its drop-in shim), and when it is loaded into the process
+// first with global visibility an ordinary link would bind this harness to
+// the shim instead of NVIDIA's libraries.  refseq_libraries() reports the
+// files the entry points come from and the libraries' versions.
+//
 // C ABI (ctypes, baseline/refseq.py); every function returns 0 on success
 // and a nonzero code with refseq_last_error() text otherwise.
+#include <dlfcn.h>
+
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cublas_v2.h>
@@ -50,6 +59,65 @@ int drv_fail(CUresult r, const char *what)
     const char *s = nullptr;
     cuGetErrorString(r, &s);
     return fail(3, std::string(what) + ": " + (s ? s : "CUDA driver error"));
+}
+
+// NVIDIA's cuFFT and cuBLAS entry points, bound from their own libraries.
+struct Vendor {
+    bool ok = false;
+    void *fft = nullptr, *blas = nullptr;
+    cufftResult (*plan1d)(cufftHandle *, int, cufftType, int) = nullptr;
+    cufftResult (*set_stream)(cufftHandle, cudaStream_t) = nullptr;
+    cufftResult (*exec_c2c)(cufftHandle, cufftComplex *, cufftComplex *, int) = nullptr;
+    cufftResult (*destroy)(cufftHandle) = nullptr;
+    cufftResult (*fft_version)(int *) = nullptr;
+    cublasStatus_t (*create)(cublasHandle_t *) = nullptr;
+    cublasStatus_t (*blas_set_stream)(cublasHandle_t, cudaStream_t) = nullptr;
+    cublasStatus_t (*blas_destroy)(cublasHandle_t) = nullptr;
+    cublasStatus_t (*blas_version)(cublasHandle_t, int *) = nullptr;
+    cublasStatus_t (*cgemm_batched)(cublasHandle_t, cublasOperation_t, cublasOperation_t, int,
+                                    int, int, const cuComplex *, const cuComplex *const[], int,
+                                    const cuComplex *const[], int, const cuComplex *,
+                                    cuComplex *const[], int, int) = nullptr;
+};
+Vendor g_vendor;
+
+void *open_first(const char *const *names)
+{
+    for (int i = 0; names[i]; i++) {
+        void *h = dlopen(names[i], RTLD_NOW | RTLD_LOCAL | RTLD_DEEPBIND);
+        if (h) return h;
+    }
+    return nullptr;
+}
+
+template <typename F>
+bool bind(void *h, const char *name, F &f)
+{
+    f = reinterpret_cast<F>(dlsym(h, name));
+    return f != nullptr;
+}
+
+int load_vendor()
+{
+    Vendor &v = g_vendor;
+    if (v.ok) return 0;
+    static const char *fft_names[] = {"libcufft.so.12", "libcufft.so", nullptr};
+    static const char *blas_names[] = {"libcublas.so.13", "libcublas.so", nullptr};
+    v.fft = open_first(fft_names);
+    if (!v.fft) return fail(6, std::string("dlopen libcufft: ") + dlerror());
+    v.blas = open_first(blas_names);
+    if (!v.blas) return fail(6, std::string("dlopen libcublas: ") + dlerror());
+    if (!bind(v.fft, "cufftPlan1d", v.plan1d) || !bind(v.fft, "cufftSetStream", v.set_stream) ||
+        !bind(v.fft, "cufftExecC2C", v.exec_c2c) || !bind(v.fft, "cufftDestroy", v.destroy) ||
+        !bind(v.fft, "cufftGetVersion", v.fft_version) ||
+        !bind(v.blas, "cublasCreate_v2", v.create) ||
+        !bind(v.blas, "cublasSetStream_v2", v.blas_set_stream) ||
+        !bind(v.blas, "cublasDestroy_v2", v.blas_destroy) ||
+        !bind(v.blas, "cublasGetVersion_v2", v.blas_version) ||
+        !bind(v.blas, "cublasCgemmBatched", v.cgemm_batched))
+        return fail(6, "dlsym: a cuFFT or cuBLAS entry point is missing");
+    v.ok = true;
+    return 0;
 }
 
 // Reference kernel symbols (C++ names of MDT_device_functions.h:44-46).
@@ -86,12 +154,34 @@ extern "C" {
 
 const char *refseq_last_error() { return g_err.c_str(); }
 
+// The files cuFFT's cufftExecC2C and cuBLAS's cublasCgemmBatched were bound
+// from (dladdr), written as "<cufft file>|<cublas file>" into `buf`, and the
+// two libraries' version numbers.
+int refseq_libraries(char *buf, int len, int *cufft_version, int *cublas_version)
+{
+    if (int rc = load_vendor()) return rc;
+    Dl_info a{}, b{};
+    dladdr(reinterpret_cast<void *>(g_vendor.exec_c2c), &a);
+    dladdr(reinterpret_cast<void *>(g_vendor.cgemm_batched), &b);
+    snprintf(buf, (size_t)len, "%s|%s", a.dli_fname ? a.dli_fname : "?",
+             b.dli_fname ? b.dli_fname : "?");
+    *cufft_version = 0;
+    *cublas_version = 0;
+    g_vendor.fft_version(cufft_version);
+    cublasHandle_t h = nullptr;
+    if (g_vendor.create(&h) == CUBLAS_STATUS_SUCCESS) {
+        g_vendor.blas_version(h, cublas_version);
+        g_vendor.blas_destroy(h);
+    }
+    return 0;
+}
+
 void refseq_destroy(RefSeq *r)
 {
     if (!r) return;
     if (r->stream) cudaStreamSynchronize(r->stream);
-    if (r->blas) cublasDestroy(r->blas);
-    if (r->fft_ok) cufftDestroy(r->fft);
+    if (r->blas) g_vendor.blas_destroy(r->blas);
+    if (r->fft_ok) g_vendor.destroy(r->fft);
     cudaFree(r->window);
     cudaFree(r->finput);
     cudaFree(r->foutput);
@@ -111,6 +201,7 @@ int refseq_create(const char *fatbin, int ne, int nch, int ntaps, int nsp, RefSe
 {
     *out = nullptr;
     if (ne <= 0 || nch <= 0 || ntaps <= 0 || nsp <= 0) return fail(1, "bad shape");
+    if (int rc = load_vendor()) return rc;
     RefSeq *r = new RefSeq;
     r->ne = ne;
     r->nch = nch;
@@ -153,13 +244,13 @@ int refseq_create(const char *fatbin, int ne, int nch, int ntaps, int nsp, RefSe
         refseq_destroy(r);
         return cuda_fail(e, "pointer arrays");
     }
-    cufftResult fr = cufftPlan1d(&r->fft, nch, CUFFT_C2C, nsp * ne);
+    cufftResult fr = g_vendor.plan1d(&r->fft, nch, CUFFT_C2C, nsp * ne);
     if (fr != CUFFT_SUCCESS) { refseq_destroy(r); return fail(4, "cufftPlan1d: " + std::to_string(fr)); }
     r->fft_ok = true;
-    cufftSetStream(r->fft, r->stream);
-    cublasStatus_t bs = cublasCreate(&r->blas);
+    g_vendor.set_stream(r->fft, r->stream);
+    cublasStatus_t bs = g_vendor.create(&r->blas);
     if (bs != CUBLAS_STATUS_SUCCESS) { refseq_destroy(r); return fail(5, "cublasCreate: " + std::to_string(bs)); }
-    cublasSetStream(r->blas, r->stream);
+    g_vendor.blas_set_stream(r->blas, r->stream);
     *out = r;
     return 0;
 }
@@ -216,7 +307,7 @@ int refseq_stage(RefSeq *r, int stage)
         return cr == CUDA_SUCCESS ? 0 : drv_fail(cr, "PpS_Batch launch");
     }
     if (stage == 1) {
-        cufftResult fr = cufftExecC2C(r->fft, (cufftComplex *)r->foutput,
+        cufftResult fr = g_vendor.exec_c2c(r->fft, (cufftComplex *)r->foutput,
                                       (cufftComplex *)r->foutput, CUFFT_FORWARD);
         return fr == CUFFT_SUCCESS ? 0 : fail(4, "cufftExecC2C: " + std::to_string(fr));
     }
@@ -228,7 +319,7 @@ int refseq_stage(RefSeq *r, int stage)
     }
     if (stage == 3) {
         cuComplex alpha = make_cuComplex(1.0f / nsp, 0.0f), beta = make_cuComplex(0.0f, 0.0f);
-        cublasStatus_t bs = cublasCgemmBatched(
+        cublasStatus_t bs = g_vendor.cgemm_batched(
             r->blas, CUBLAS_OP_N, CUBLAS_OP_C, ne, ne, nsp, &alpha,
             (const cuComplex *const *)r->xin_ptr, ne, (const cuComplex *const *)r->xin_ptr, ne,
             &beta, (cuComplex *const *)r->xout_ptr, ne, nch);

@@ -8,7 +8,9 @@ NVIDIA's cuFFT and cuBLAS exactly as the reference client's rank 2 calls them
 parity check and bench.py times it as the library bar.
 
 build() compiles refseq.cu into baseline/_build/librefseq.so (nvcc, sm_103a,
-linked against libcuda, libcufft and libcublas).
+linked against libcuda; cuFFT and cuBLAS are opened at run time with
+dlopen(RTLD_LOCAL | RTLD_DEEPBIND), so that their entry points cannot be
+bound to the same-named shim that libmdtfx.so exports).
 """
 import ctypes
 import os
@@ -43,7 +45,7 @@ def build(force=False):
     cmd = [_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17",
            "-Xcompiler", "-fPIC", "-shared", "-o", tmp, SRC,
            "-L", os.path.join(cuda, "lib64"), "-L", os.path.join(cuda, "lib64", "stubs"),
-           "-lcuda", "-lcufft", "-lcublas"]
+           "-lcuda", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("refseq build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
@@ -74,12 +76,24 @@ def lib():
         L.refseq_run.argtypes = [P, I, I, ctypes.POINTER(ctypes.c_float),
                                  ctypes.POINTER(ctypes.c_float)]
         L.refseq_window_bh.argtypes = [P, P]
+        L.refseq_libraries.argtypes = [ctypes.c_char_p, I, ctypes.POINTER(I), ctypes.POINTER(I)]
         _lib = L
     return _lib
 
 
 class RefSeqError(RuntimeError):
     pass
+
+
+def libraries():
+    """(cuFFT file, cuBLAS file, cuFFT version, cuBLAS version) of the entry
+    points the harness calls."""
+    buf = ctypes.create_string_buffer(4096)
+    fv, bv = ctypes.c_int(), ctypes.c_int()
+    _check(lib().refseq_libraries(buf, 4096, ctypes.byref(fv), ctypes.byref(bv)),
+           "refseq_libraries")
+    a, _, b = buf.value.decode().partition("|")
+    return a, b, fv.value, bv.value
 
 
 def _check(rc, what):

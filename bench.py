@@ -537,7 +537,8 @@ def e2e_run(mdt, cfg, precision, dev, iq, vis_dev, samples, steps, barrier, loca
            "h2d_bytes_per_step": int(h_iq.numel()), "d2h_bytes_per_step": int(h_vis.numel() * 4),
            "matches_device_run": None if ok is None else bool(ok), "host_cpus": host_cpus,
            "steps": steps, "statistic": "median step",
-           "ms_per_step_min": srt[0] * 1e3, "ms_per_step_max": srt[-1] * 1e3}
+           "ms_per_step_min": srt[0] * 1e3, "ms_per_step_max": srt[-1] * 1e3,
+           "ms_per_step_all": [round(x * 1e3, 2) for x in times]}
     os.sched_setaffinity(0, all_cpus)  # the CPU baseline uses every core
     del h_iq, h_vis
     return res
@@ -656,26 +657,34 @@ def run_ours(args, cfg):
         e2e.update(r)
 
     extras = {}
-    if rank == 0 and not args.no_extras:
+    want = set()
+    if not args.no_extras:
+        want = set(("accuracy,paths,link,station_c2,library_bar,batched,differentiation"
+                    if args.sections == "all" else args.sections).split(","))
+    if rank == 0 and "accuracy" in want:
         extras["accuracy"] = accuracy_section(mdt, cfg, dev, iq, win, vis, precision)
     del vis
     torch.cuda.empty_cache()
-    if not args.no_extras:
+    if "paths" in want:
         extras.update(paths_section(mdt, cfg, dev, iq, win, ms, precision,
                                     max(1, min(args.steps, 3))))
     del iq
     torch.cuda.empty_cache()
-    if not args.no_extras:
+    if "link" in want:
         extras["link"] = link_section(dev)
         if e2e is not None:
             h2d = extras["link"]["h2d_gbs"]
             e2e["link_floor_value"] = samples / (e2e["h2d_bytes_per_step"] / (h2d * 1e9))
             e2e["link_note"] = ("inputs alone at the link's measured H2D rate; e2e is "
                                 "link-bound when value is near this")
+    if "station_c2" in want:
         extras["station_c2"] = station_section(mdt, dev, max(1, min(args.steps, 5)), barrier,
                                                local, not args.no_e2e)
+    if "library_bar" in want:
         extras["library_bar"] = library_bar_section(mdt, dev)
+    if "batched" in want:
         extras["batched"] = batch_section(mdt, dev, steps=max(1, min(args.steps, 5)))
+    if "differentiation" in want:
         extras["differentiation"] = gaincal_section(mdt, dev, steps=max(1, min(args.steps, 10)))
 
     line = None
@@ -784,9 +793,12 @@ def library_bar_section(mdt, dev):
     from baseline import refseq
     if not refseq.available():
         return {"unavailable": "reference kernels not compiled (baseline/build_ref_gpu.sh)"}
+    fft_file, blas_file, fft_ver, blas_ver = refseq.libraries()
     out = {"what": "reference kernels (sm_103a build of MDT_device_functions.cu) + cuFFT + "
                    "cuBLAS, launched as MDT_OneStation_client.cu:1083-1170 does, one "
-                   "integration per rep; complex64 input converted exactly from the int8 I/Q"}
+                   "integration per rep; complex64 input converted exactly from the int8 I/Q",
+           "libraries": {"cufft": fft_file, "cufft_version": fft_ver, "cublas": blas_file,
+                         "cublas_version": blas_ver}}
     for cfg, tensor_prec in ((mdt.configs.C2, None), (mdt.configs.C3, "fp16")):
         one = mdt.configs.small(cfg, nint=1)
         ne, nch, ntaps, nsp = one.nelements, one.nchannels, one.ntaps, one.nspectra
@@ -893,11 +905,11 @@ def gaincal_section(mdt, dev, steps):
     torch.cuda.synchronize()
     t0 = time.time()
     g, hist = adj.solve_gains(iq_model, win, data, model, ne, nch, ntaps, nsp, iters=400,
-                              tol=1e-13, true_gains=g_true)
+                              tol=1e-13, gtol=1e-7, true_gains=g_true)
     torch.cuda.synchronize()
     wall = time.time() - t0
     g_min, _ = adj.solve_gains(iq_model, win, data, model, ne, nch, ntaps, nsp, iters=400,
-                               tol=1e-13, g0=g_true)
+                               tol=1e-13, gtol=1e-7, g0=g_true)
     err = adj.gain_error(g, g_true)
     return {"workload": c5.name, "fwd_bwd_ms": ms,
             "fwd_bwd_value": c5.antenna_samples() / (ms * 1e-3), "unit": "antenna-samples/s",
@@ -927,6 +939,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e run")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the headline measurement (profiling runs)")
+    ap.add_argument("--sections", default="all",
+                    help="comma-separated extra sections to run (accuracy, paths, link, "
+                         "station_c2, library_bar, batched, differentiation) or all")
     ap.add_argument("--precision", choices=list(PREC), default="fp16",
                     help="plan precision of the main measurement")
     ap.add_argument("--nspectra", type=int, default=None,

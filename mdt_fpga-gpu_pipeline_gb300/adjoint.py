@@ -122,7 +122,7 @@ def gain_error(est, true):
 
 
 def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9, step=0.5,
-                true_gains=None, callback=None, g0=None):
+                true_gains=None, callback=None, g0=None, gtol=1e-7):
     """Per-antenna, per-channel complex gains by gradient descent.
 
     Loss  L(g) = sum_c sum_{a<b} |data_ab - V(g)_ab|^2,  V(g) = the FX
@@ -135,9 +135,10 @@ def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9,
     (channel, antenna) by the diagonal of the Gauss-Newton normal equations,
         h_ca = sum_{b != a} |g_cb|^2 |model_c,ab|^2,
     computed with the iterate in FP64 on the GPU:  g <- g - step * grad / (2h).
-    Starts from `g0` (default unit gains); stops when the relative loss
-    change between steps drops below `tol`, or the relative loss itself does
-    (or after `iters` steps).  Returns (gains complex64 [Nch, NE], history
+    Starts from `g0` (default unit gains); stops when the relative loss drops
+    below `tol` (data the model explains exactly), when a step changes the
+    gains by less than `gtol` relative (the minimiser of a noisy loss), or
+    after `iters` steps.  Returns (gains complex64 [Nch, NE], history
     list of (relative loss, error against true_gains or None))."""
     dev = iq.device
     mask = baseline_mask(ne, dev)
@@ -158,12 +159,14 @@ def solve_gains(iq, taps, data, model, ne, nch, ntaps, nsp, iters=200, tol=1e-9,
         hist.append((float(loss.detach()) / dnorm, err))
         if callback is not None:
             callback(len(hist), hist[-1])
-        if hist[-1][0] < tol or (len(hist) > 1 and
-                                 abs(hist[-2][0] - hist[-1][0]) <= tol * hist[-1][0]):
+        if hist[-1][0] < tol:
             break
         gg = g.real ** 2 + g.imag ** 2
         h = (m2 * gg[:, None, :]).sum(dim=2)  # model is Hermitian: |M_ab| = |M_ba|
-        g = g - step * gv.grad.to(torch.complex128) / (2 * h)
+        dg = step * gv.grad.to(torch.complex128) / (2 * h)
+        g = g - dg
+        if float(_sqnorm(dg)) <= gtol ** 2 * float(_sqnorm(g)):
+            break
     return g.to(torch.complex64), hist
 
 

@@ -12,8 +12,8 @@ Nch-1 and 13 seeded ones) against the FP64 oracle run on the same samples:
     sum of the oracle's per-integration visibilities (<= 1e-3), and against
     the sum of the plan's own per-integration outputs (<= 1e-12).
 Configuration 4 in full: the 24 ragged_jobs() in one graph-captured batch,
-replayed, against single-job plans (<= 1e-6) and the FP64 oracle on 3
-channels per job (<= 1e-3).
+replayed, bit-equal to single-job plans and within 1e-3 of the FP64 oracle
+on 3 channels per job.
 The oracle's cost is bounded by the channel subset; the F-engine rows of
 every (spectrum, element) are still computed in FP64."""
 import numpy as np
@@ -207,12 +207,12 @@ def test_c4_all_ragged_jobs(mdt, oracle, cuda):
         plan.close()
         v = vis[k].cpu().numpy()
         assert np.all(np.isfinite(v)), j.name
+        assert torch.equal(vis[k].view(torch.int64), ref.view(torch.int64)), j.name
         e_plan = rel_fro(v, ref.cpu().numpy().astype(np.complex128))
         sel = [0, nch // 3, nch - 1]
         o = oracle.fx(iqs[k].cpu().numpy(), win.cpu().numpy(), ne, nch, nt, nsp, channels=sel)
         e_or = rel_fro(v[sel], o)
         worst_plan, worst_oracle = max(worst_plan, e_plan), max(worst_oracle, e_or)
-        assert e_plan < 1e-6, (j.name, e_plan)
         assert e_or < TOL_F16, (j.name, e_or)
     print("c4 24 jobs: batch vs single plans max %.2e, vs FP64 max %.2e"
           % (worst_plan, worst_oracle))

@@ -34,6 +34,11 @@ def _refseq():
     if not refseq.available():
         pytest.skip("reference kernels not compiled (baseline/build_ref_gpu.sh needs the "
                     "reference checkout)")
+    # the harness must call NVIDIA's libraries, not libmdtfx.so's same-named shim
+    fft_file, blas_file, fft_ver, blas_ver = refseq.libraries()
+    print("cuFFT %d from %s; cuBLAS %d from %s" % (fft_ver, fft_file, blas_ver, blas_file))
+    assert "libcufft" in fft_file and "libcublas" in blas_file
+    assert "mdtfx" not in fft_file + blas_file
     return refseq
 
 

@@ -15,10 +15,15 @@ def test_refseq_harness_builds_and_exports():
                           text=True).stdout
     for name in ("refseq_create", "refseq_destroy", "refseq_set_input", "refseq_stage",
                  "refseq_run", "refseq_read", "refseq_ptr", "refseq_window_bh",
-                 "refseq_last_error"):
+                 "refseq_last_error", "refseq_libraries"):
         assert name in syms, name
+    # cuFFT and cuBLAS are opened at run time from their own files, never
+    # bound at load time (where libmdtfx.so's same-named shim could win)
     deps = subprocess.run(["readelf", "-d", lib], capture_output=True, text=True).stdout
-    assert "libcufft" in deps and "libcublas" in deps
+    assert "libcufft" not in deps and "libcublas" not in deps
+    undef = subprocess.run(["nm", "-D", "--undefined-only", lib], capture_output=True,
+                           text=True).stdout
+    assert "cufftExecC2C" not in undef and "cublasCgemmBatched" not in undef
 
 
 def test_reference_gpu_recipe_skips_without_checkout():
