@@ -13,17 +13,17 @@
 //   Y[k1][n2] = sum_n1 P[32 n1 + n2] w_32^{n1 k1}                  (MMA 1)
 //   Z[k1][n2] = Y[k1][n2] w_1024^{n2 k1}                            (FP32)
 //   X[k1 + 32 k2] = sum_n2 Z[k1][n2] w_32^{n2 k2}                   (MMA 2)
-// Both products are real GEMMs M = 128, N = 64, K = 64 over interleaved
-// (re, im) pairs: MMA 1 rows are (spectrum, n2), K is n1; MMA 2 rows are
-// (spectrum, k1), K is n2; B is the same real 64 x 64 form of the 32-point
-// DFT matrix for both.
+// Both are real GEMMs over interleaved (re, im) pairs with the real 64 x 64
+// form of the 32-point DFT matrix.  MMA 1: M = 128 rows (spectrum, n2), K =
+// n1, N = 64 (k1); the DFT matrix is the B operand.  MMA 2 is transposed so
+// that each output channel's spectra land along one TMEM lane: D = A Z^T
+// with A = blockdiag(DFT, DFT) (M = 128 rows: (k2, re|im) for k1 < 16, then
+// for k1 >= 16; K = 128) and Z as the B operand (N = 128 rows (k1 mod 16,
+// spectrum), K = [n2 of k1 | n2 of k1 + 16]).  A thread reading TMEM lane
+// (k2, re|im) then holds 8 consecutive spectra of one component of a channel
+// per 8 columns: one 16-byte chunk of the X16 output, converted and stored
+// straight from registers.
 //
-// Work: one CTA per SM walks runs of up to 256 spectra of one element in
-// units of 8 spectra (two 128-row MMA tiles).  Warps 0-7 carry the last
-// Ntaps-1 converted input rows in tensor memory, so every input sample is
-// loaded (bulk copy of 2 KB rows into a two-slot shared-memory ring) and
-// converted once; warps 8-23 run the twiddle and output stages of the
-// previous unit meanwhile (see fengine_tc_kernel).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -39,27 +39,48 @@ namespace ftc {
 constexpr int N = 1024;
 constexpr int PT = 256;                 // PFB threads (warps 0-7)
 constexpr int ET = 512;                 // epilogue threads (warps 8-23)
-constexpr int THREADS = PT + ET;
+constexpr int THREADS = PT + ET + 64;   // + the loader (warp 24) and MMA (warp 25) warps
+constexpr int NSLOT = 4;                // input ring slots
 constexpr int US = 8;                   // spectra per unit
 constexpr int CPT = N / PT;             // channels per PFB thread
 constexpr int ROWB = 2 * N;             // one (spectrum, element) row of int8 I/Q
 constexpr int RUN = 256;                // spectra per work item
 constexpr uint32_t TILE = 16384;        // 128 rows x 128 bytes
-// shared memory: DFT matrix, twiddles, int8 requantisation scales, scaled
-// window, two P operand buffers (two tiles each), the Z operand, the output
-// staging S, the input ring (two slots of 8 rows)
-constexpr uint32_t OFF_B = 0, OFF_TW = 8192, OFF_QS = 16384, OFF_W = 20480;
-constexpr uint32_t OFF_P = 53248, OFF_Z = OFF_P + 4 * TILE, OFF_S = OFF_Z + 2 * TILE;
-constexpr uint32_t OFF_RING = OFF_S + 2 * TILE;
-constexpr uint32_t SMEM = OFF_RING + 2 * US * ROWB;
-// TMEM columns: two accumulator buffers of two 64-column tiles (MMA 1 of unit
-// u writes buffer u % 2, MMA 2 of the same unit overwrites it once the
-// twiddle stage has read it), 64 columns holding the packed output of the
-// first 8 spectra of each 16-spectrum pair, and the PFB carry: per PFB thread
-// and channel the last Ntaps-1 converted input rows (16 columns).
+// shared memory: the 128 x 128 block-diagonal DFT operand of MMA 2 as two
+// 128-row tiles of K 64 (the first 64 rows of the first tile are MMA 1's
+// B operand), twiddles, int8 requantisation scales, scaled window, two
+// operand buffers of two tiles each (unit u's P tiles, read by MMA 1, then
+// its Z tiles -- k1 < 16 and k1 >= 16 -- read by MMA 2), the input ring
+// (NSLOT slots of 8 rows)
+constexpr uint32_t OFF_B = 0, OFF_B2 = 16384, OFF_TW = 32768, OFF_QS = 40960, OFF_W = 45056;
+constexpr uint32_t OFF_P = 77824;
+constexpr uint32_t OFF_RING = OFF_P + 4 * TILE;
+constexpr uint32_t SMEM = OFF_RING + NSLOT * US * ROWB;
+// TMEM columns: two accumulator buffers of 128 columns (MMA 1 of unit u
+// writes buffer u % 2 as two 64-column tiles, MMA 2 of the same unit
+// overwrites all 128 columns once the twiddle stage has read them), the
+// packed output chunks of the first unit of each pair of 8-spectrum units
+// (16 columns per epilogue thread), and the PFB carry: per PFB thread and
+// channel the last Ntaps-1 converted input rows (16 columns).
 constexpr uint32_t TMEM_COLS = 512, T_D = 0, T_STASH = 256, T_CARRY = 320;
-// mbarriers
-enum { BAR_RING = 0, BAR_MMA1 = 2, BAR_FREE = 4, BAR_MMA2 = 6, NBARS = 7 };
+// mbarriers (per ring slot, or per operand / accumulator buffer, so that no
+// waiter is ever more than one phase behind): ring slot filled (bulk copies
+// landed) / emptied (PFB has read it); P written; MMA 1 done; Z written;
+// MMA 2 done (accumulators readable); operand buffer free (MMA 2 has read Z);
+// accumulator buffer free (the epilogue has read MMA 2's result)
+enum {
+    BAR_FULL = 0, BAR_EMPTY = NSLOT, BAR_PFULL = 2 * NSLOT, BAR_MMA1 = 2 * NSLOT + 2,
+    BAR_ZFULL = 2 * NSLOT + 4, BAR_MMA2 = 2 * NSLOT + 6, BAR_PFREE = 2 * NSLOT + 8,
+    BAR_DFREE = 2 * NSLOT + 10, NBARS = 2 * NSLOT + 12
+};
+__host__ __device__ constexpr uint32_t bar_count(int b)
+{
+    return (b >= BAR_EMPTY && b < BAR_EMPTY + NSLOT) || (b >= BAR_PFULL && b < BAR_PFULL + 2)
+               ? PT
+               : ((b >= BAR_DFREE && b < BAR_DFREE + 2) || (b >= BAR_ZFULL && b < BAR_ZFULL + 2)
+                      ? ET
+                      : 1);
+}
 
 // One launch: a single job (with optional PFB history) or a device table of
 // jobs (FJob, work items from wk0).
@@ -121,11 +142,11 @@ __device__ __forceinline__ float2 lds_f2(uint32_t a)
     asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
     return v;
 }
-// One 32-byte (full sector) global store.
-__device__ __forceinline__ void stg32(void *p, const uint4 &a, const uint4 &b)
+// One 32-byte (full sector) global store of two 16-byte chunks.
+__device__ __forceinline__ void stg32(void *p, const uint32_t *lo, const uint32_t *hi)
 {
-    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(a.x),
-                 "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(lo[0]),
+                 "r"(lo[1]), "r"(lo[2]), "r"(lo[3]), "r"(hi[0]), "r"(hi[1]), "r"(hi[2]), "r"(hi[3])
                  : "memory");
 }
 // Position of channel c's window pair in the shared window table: channels
@@ -169,17 +190,19 @@ __device__ __forceinline__ uint32_t pack_h2<__nv_bfloat16>(float re, float im)
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
+// Two consecutive spectra (a, b) of one component -> one 32-bit word of the
+// X16 row (a in the low half).
 template <int MODE>
-__device__ __forceinline__ uint32_t pack_out(float re, float im, float qs)
+__device__ __forceinline__ uint32_t pack_out(float a, float b, float qs)
 {
     if constexpr (MODE == OUT_Q8) {
-        re = fminf(fmaxf(rintf(re * qs), -127.0f), 127.0f);
-        im = fminf(fmaxf(rintf(im * qs), -127.0f), 127.0f);
-        return pack_h2<__half>(re, im);
+        a = fminf(fmaxf(rintf(a * qs), -127.0f), 127.0f);
+        b = fminf(fmaxf(rintf(b * qs), -127.0f), 127.0f);
+        return pack_h2<__half>(a, b);
     } else if constexpr (MODE == OUT_BF16) {
-        return pack_h2<__nv_bfloat16>(re, im);
+        return pack_h2<__nv_bfloat16>(a, b);
     } else {
-        return pack_h2<__half>(re, im);
+        return pack_h2<__half>(a, b);
     }
 }
 
@@ -241,22 +264,25 @@ __device__ __forceinline__ Item item_of(const FJob &a, int w)
     return it;
 }
 
-// One staged unit waiting for its copy-out.
-struct OutUnit {
-    uint8_t *X16;
-    int nep, e, kc, j0, nvalid;
-    bool second, lone;
-};
-
-// Warp-specialised pipeline, one CTA per SM.  Warps 0-7 (PFB role) stream
-// the input, run the tap sum into P buffer u % 2 (the tap carry lives in
-// TMEM) and issue MMA 1 into TMEM accumulator buffer u % 2.  Warps 8-23
-// (epilogue role) read that buffer, apply the twiddles into Z, issue MMA 2
-// into the same buffer, store the previous unit (from the staging buffer S)
-// while MMA 2 works, then pack this unit's result into S.  The roles meet
-// only at mbarriers: MMA 1 done (P written, accumulators ready) and buffer
-// free (the epilogue has read MMA 2's result), so the PFB of unit u + 1 runs
-// while the epilogue of unit u works.
+// Warp-specialised pipeline, one CTA per SM, four roles that meet only at
+// mbarriers (no named barrier between warps):
+//  * loader (warp 24, one thread): the bulk copies of the input rows into an
+//    NSLOT-slot ring, up to NSLOT uses ahead of the PFB;
+//  * MMA issuer (warp 25, one thread): MMA 2 of each unit once its Z tiles
+//    are written (first, the epilogue waits on it), MMA 1 once its P tiles
+//    are written and its accumulator buffer is free; it polls both
+//    conditions without blocking on either;
+//  * PFB (warps 0-7): per ring use, either a work item's Ntaps-1 lead-in rows
+//    into the tap carry (TMEM) or one unit's tap sum into operand buffer
+//    u % 2, once MMA 2 of unit u - 2 has read that buffer;
+//  * epilogue (warps 8-23), pipelined over two units: the twiddle stage of
+//    unit u from MMA 1's accumulators into Z (operand buffer u % 2, whose P
+//    tiles MMA 1 has consumed), then the output of unit u - 1 (MMA 2's
+//    result, converted and stored) while MMA 2 of unit u runs.
+// Every wait is bounded and warp-uniform (the warp's lanes agree before
+// acting); a failed wait raises the CTA's abort flag, which ends every other
+// wait early, and the roles leave their loops without further tensor-memory
+// traffic.
 template <int NT, int MODE>
 __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
 {
@@ -264,7 +290,6 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     __shared__ uint64_t bars[NBARS];
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
-    __shared__ OutUnit prev_s;  // the epilogue's staged unit awaiting its copy-out
 
     const uint32_t sbase = tc::smem_u32(sm);
     const int tid = threadIdx.x;
@@ -275,16 +300,22 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     }
 
     // ---------------------------------------------------------------- setup
-    for (int i = tid; i < 64 * 64; i += THREADS) {
-        // 32-point DFT matrix, real form: row kout = 2 k + (re|im), column kin = 2 n + (re|im)
-        const int kout = i >> 6, kin = i & 63;
-        const int k = kout >> 1, n = kin >> 1;
-        float s, c;
-        sincospif((float)((n * k) & 31) / 16.0f, &s, &c);
-        const float v = (kout & 1) ? ((kin & 1) ? c : -s) : ((kin & 1) ? s : c);
-        const __half hv = __float2half_rn(v);
-        *reinterpret_cast<__half *>(sm + OFF_B + kout * 128 +
-                                    (((kin >> 3) ^ (kout & 7)) << 4) + ((kin & 7) << 1)) = hv;
+    for (int i = tid; i < 128 * 128; i += THREADS) {
+        // block-diagonal real form of the 32-point DFT matrix: row r =
+        // 64 h + 2 k + (re|im), column K = 64 h' + 2 n + (re|im), zero unless
+        // h == h'; stored as two K-major 128-byte-swizzled tiles (K 0-63, 64-127)
+        const int r = i >> 7, K = i & 127;
+        const int kout = r & 63, kin = K & 63;
+        float v = 0.0f;
+        if ((r >> 6) == (K >> 6)) {
+            const int k = kout >> 1, n = kin >> 1;
+            float s, c;
+            sincospif((float)((n * k) & 31) / 16.0f, &s, &c);
+            v = (kout & 1) ? ((kin & 1) ? c : -s) : ((kin & 1) ? s : c);
+        }
+        *reinterpret_cast<__half *>(sm + OFF_B + (uint32_t)(K >> 6) * TILE + r * 128 +
+                                    (((kin >> 3) ^ (r & 7)) << 4) + ((kin & 7) << 1)) =
+            __float2half_rn(v);
     }
     float2 *tw = reinterpret_cast<float2 *>(sm + OFF_TW);
     for (int i = tid; i < 32 * 32; i += THREADS) {
@@ -296,9 +327,10 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     float *qs_s = reinterpret_cast<float *>(sm + OFF_QS);
     if constexpr (MODE == OUT_Q8)
         for (int i = tid; i < N; i += THREADS) qs_s[i] = __ldg(L.qscales + i);
+    const uint32_t bar0 = tc::smem_u32(&bars[0]);
+    auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
     if (tid == 0) {
-        for (int b = 0; b < NBARS; b++)
-            tc::mbar_init(tc::smem_u32(&bars[b]), (b == BAR_FREE || b == BAR_FREE + 1) ? ET : 1);
+        for (int b = 0; b < NBARS; b++) tc::mbar_init(bar(b), bar_count(b));
         abort_flag = 0;
         tc::fence_mbar_init();
     }
@@ -312,119 +344,81 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
     volatile int *abortp = &abort_flag;
-    // A failed wait raises the CTA's abort flag (which ends the other role's
-    // waits early) and the thread's own flag; each role leaves its loop only
-    // at a barrier that ORs the threads' flags, so all its threads leave
-    // together and none is left at a named barrier.
-    bool bad = false;
     auto fail = [&]() {
         atomicExch(L.err, 1);
         *abortp = 1;
-        bad = true;
     };
-    const uint32_t id_mma = tc::idesc_f16(64, 0, 0);  // M 128, N 64, f16 operands
-    const uint64_t bdesc = tc::sw128_kmajor_desc(sbase + OFF_B);
-    const uint32_t bar_mma1 = tc::smem_u32(&bars[BAR_MMA1]);    // + 8 * b
-    const uint32_t bar_free = tc::smem_u32(&bars[BAR_FREE]);  // + 8 * b
-    const uint32_t bar_mma2 = tc::smem_u32(&bars[BAR_MMA2]);
-    const uint32_t gZ = sbase + OFF_Z;
+    // bounded wait whose outcome every lane of the warp shares
+    auto wait_warp = [&](uint32_t b, uint32_t parity) {
+        const bool okw = wait_or_abort(b, parity, abortp);
+        return __all_sync(0xffffffffu, okw);
+    };
+    const uint32_t gR = sbase + OFF_RING;
 
     if (tid < PT) {
         // ============================================================ PFB role
         const int t = tid, wg = t >> 5, l = t & 31;
-        const uint32_t gR = sbase + OFF_RING;
         // scaled window, tap pairs: wsp[p][wpos(c)] = (W[2p][c], W[2p+1][c]) * scale
         float2 *wsp = reinterpret_cast<float2 *>(sm + OFF_W);
         const uint32_t wsp_s = sbase + OFF_W;
-        const uint32_t bar_in0 = tc::smem_u32(&bars[BAR_RING]), bar_in1 = bar_in0 + 8;
-        uint32_t ph_in0 = 0, ph_in1 = 0;
-        bool pend0 = false, pend1 = false;  // loads in flight (for the drain on abort)
-        const bool issuer = (t == 0);
-        long last_mma = -1;
         // carry of channel j: TMEM columns carry_t + 16 j (words 2i, 2i + 1 = row i)
         const uint32_t carry_t = tmem + ((uint32_t)((wg & 3) * 32) << 16) + T_CARRY + (uint32_t)((wg >> 2) * 64);
         bool ok = true;
-        long n = 0;  // units of this CTA so far
+        long n = 0, r = 0;  // units and ring uses of this CTA so far
         FJob a = L.one;
         int cur = -1;
-        const int nhist = L.table ? 0 : L.nhist;
-        auto row_src = [&](long rho, int e) -> const char2 * {
-            return rho < nhist ? L.hist + (rho * a.ne + e) * (long)N
-                               : a.iq + ((rho - nhist) * a.ne + e) * (long)N;
-        };
-        // issue the bulk copies of rows [r0, r0 + cnt) of element e into slot s
-        auto load_rows = [&](int s, long r0, int cnt, int e) {
-            const uint32_t bar = s ? bar_in1 : bar_in0;
-            tc::mbar_expect_tx(bar, (uint32_t)(cnt * ROWB));
-            for (int r = 0; r < cnt; r++)
-                tc::bulk_g2s(gR + (uint32_t)(s * 8 * ROWB + r * ROWB), row_src(r0 + r, e), ROWB, bar);
-        };
-        auto sync_pfb = [&]() { tc::named_barrier(1, PT); };
-        auto sync_pfb_bad = [&]() { return tc::named_barrier_or(1, PT, bad); };
-
         for (int w = blockIdx.x; w < L.nwork && ok; w += gridDim.x) {
             if (next_job(L, w, a, cur)) {
-                sync_pfb();  // the previous job's window is no longer read
-                for (int i = t; i < N * 4; i += PT) {
-                    const int pr = i >> 10, c = i & (N - 1);
-                    const float w0 = 2 * pr < NT ? __ldg(a.win + 2 * pr * N + c) * a.scale : 0.0f;
-                    const float w1 =
-                        2 * pr + 1 < NT ? __ldg(a.win + (2 * pr + 1) * N + c) * a.scale : 0.0f;
-                    wsp[pr * N + wpos(c)] = make_float2(w0, w1);
+                // the job's scaled window for this thread's own channels (only this thread reads them)
+#pragma unroll
+                for (int j = 0; j < CPT; j++) {
+                    int n1, n2;
+                    chan_of(8 * j + wg, l, n1, n2);
+                    const int c = 32 * n1 + n2;
+#pragma unroll
+                    for (int pr = 0; pr < NT / 2; pr++)
+                        wsp[pr * N + wpos(c)] = make_float2(__ldg(a.win + 2 * pr * N + c) * a.scale,
+                                                            __ldg(a.win + (2 * pr + 1) * N + c) * a.scale);
                 }
-                sync_pfb();
             }
             const Item it = item_of(a, w);
-            const int e = it.e, s0 = it.s0, nunits = it.nunits;
-            auto unit_rows = [&](int u) {
-                const int r = a.nsp - s0 - US * u;
-                return r < 0 ? 0 : (r > US ? US : r);
-            };
-            // lead-in rows into slot 1, unit 0 into slot 0
-            if (issuer) {
-                load_rows(1, s0, NT - 1, e);
-                load_rows(0, s0 + NT - 1, unit_rows(0), e);
-            }
-            pend0 = pend1 = true;
-            if (!wait_or_abort(bar_in1, ph_in1, abortp)) fail();
-            ph_in1 ^= 1;
-            pend1 = false;
-#pragma unroll
-            for (int j = 0; j < CPT; j++) {
-                int n1, n2;
-                chan_of(8 * j + wg, l, n1, n2);
-                const uint32_t cb = (uint32_t)(2 * (32 * n1 + n2));
-                uint32_t cv[16] = {};
-#pragma unroll
-                for (int i = 0; i < NT - 1; i++) {
-                    const float2 x = up2(iq_to_f2(lds_u16(gR + (uint32_t)(8 * ROWB + i * ROWB) + cb)));
-                    cv[2 * i] = __float_as_uint(x.x);
-                    cv[2 * i + 1] = __float_as_uint(x.y);
-                }
-                tc::tmem_st16(carry_t + (uint32_t)(16 * j), cv);
-            }
-            tc::tmem_st_wait();
-            if (sync_pfb_bad()) {
-                ok = false;
-                break;
-            }
-            if (issuer && nunits > 1) load_rows(1, s0 + US + NT - 1, unit_rows(1), e);
-            pend1 = nunits > 1;
-
-            for (int u = 0; u < nunits; u++, n++) {
-                const int slot = u & 1, b = (int)(n & 1);
-                const uint32_t ring = gR + (uint32_t)(slot * 8 * ROWB);
-                if (!wait_or_abort(slot ? bar_in1 : bar_in0, slot ? ph_in1 : ph_in0, abortp)) fail();
-                if (slot) {
-                    ph_in1 ^= 1;
-                    pend1 = false;
-                } else {
-                    ph_in0 ^= 1;
-                    pend0 = false;
-                }
-                // P buffer b is free once MMA 1 of unit n - 2 has completed
-                if (n >= 2 && !wait_or_abort(bar_mma1 + 8 * b, (uint32_t)(((n >> 1) & 1) ^ 1), abortp))
+            const int nunits = it.nunits;
+            {  // ---- lead-in use: the item's first Ntaps-1 rows into the carry
+                const int slot = (int)(r % NSLOT);
+                if (!wait_warp(bar(BAR_FULL + slot), (uint32_t)((r / NSLOT) & 1))) {
                     fail();
+                    ok = false;
+                    break;
+                }
+                const uint32_t ring = gR + (uint32_t)(slot * US * ROWB);
+#pragma unroll
+                for (int j = 0; j < CPT; j++) {
+                    int n1, n2;
+                    chan_of(8 * j + wg, l, n1, n2);
+                    const uint32_t cb = (uint32_t)(2 * (32 * n1 + n2));
+                    uint32_t cv[16] = {};
+#pragma unroll
+                    for (int i = 0; i < NT - 1; i++) {
+                        const float2 x = up2(iq_to_f2(lds_u16(ring + (uint32_t)(i * ROWB) + cb)));
+                        cv[2 * i] = __float_as_uint(x.x);
+                        cv[2 * i + 1] = __float_as_uint(x.y);
+                    }
+                    tc::tmem_st16(carry_t + (uint32_t)(16 * j), cv);
+                }
+                tc::tmem_st_wait();
+                tc::mbar_arrive(bar(BAR_EMPTY + slot));
+                r++;
+            }
+            for (int u = 0; u < nunits; u++, n++, r++) {
+                const int slot = (int)(r % NSLOT), b = (int)(n & 1);
+                const uint32_t ring = gR + (uint32_t)(slot * US * ROWB);
+                if (!wait_warp(bar(BAR_FULL + slot), (uint32_t)((r / NSLOT) & 1)) ||
+                    // operand buffer b is free once MMA 2 of unit n - 2 has read its Z
+                    (n >= 2 && !wait_warp(bar(BAR_PFREE + b), (uint32_t)(((n >> 1) & 1) ^ 1)))) {
+                    fail();
+                    ok = false;
+                    break;
+                }
                 const uint32_t gP = sbase + OFF_P + (uint32_t)b * 2 * TILE;
                 // ---- PFB: 8 spectra x 4 channels per thread -> P tiles (f16, scaled)
 #pragma unroll
@@ -443,20 +437,20 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     }
                     uint64_t xw[NT - 1 + US];
 #pragma unroll
-                    for (int r = 0; r < US; r++)
-                        xw[NT - 1 + r] = iq_to_f2(lds_u16(ring + (uint32_t)(r * ROWB + 2 * c)));
+                    for (int q = 0; q < US; q++)
+                        xw[NT - 1 + q] = iq_to_f2(lds_u16(ring + (uint32_t)(q * ROWB + 2 * c)));
                     tc::tmem_ld_wait();
 #pragma unroll
                     for (int i = 0; i < NT - 1; i++)
                         xw[i] = pk2(__uint_as_float(cv[2 * i]), __uint_as_float(cv[2 * i + 1]));
 #pragma unroll
-                    for (int s = 0; s < US; s++) {
-                        uint64_t acc = mul2(xw[s], w2[0]);
+                    for (int sp = 0; sp < US; sp++) {
+                        uint64_t acc = mul2(xw[sp], w2[0]);
 #pragma unroll
-                        for (int i = 1; i < NT; i++) acc = fma2(xw[s + i], w2[i], acc);
+                        for (int i = 1; i < NT; i++) acc = fma2(xw[sp + i], w2[i], acc);
                         const float2 p = up2(acc);
-                        const int row = (s & 3) * 32 + n2;
-                        sts_u32(gP + (uint32_t)(s >> 2) * TILE + tile_word(row, n1),
+                        const int row = (sp & 3) * 32 + n2;
+                        sts_u32(gP + (uint32_t)(sp >> 2) * TILE + tile_word(row, n1),
                                 pack_h2<__half>(p.x, p.y));
                     }
 #pragma unroll
@@ -468,146 +462,118 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     tc::tmem_st16(carry_t + (uint32_t)(16 * j), cv);
                 }
                 tc::tmem_st_wait();  // the next unit reads the carry back
-                tc::fence_proxy_async();
-                if (sync_pfb_bad()) {
-                    ok = false;
-                    break;
-                }
-                if (issuer) {
-                    if (u + 2 < nunits) load_rows(slot, s0 + US * (u + 2) + NT - 1, unit_rows(u + 2), e);
-                    // accumulator buffer b is free once the epilogue has read unit n - 2
-                    if (n >= 2 && !wait_or_abort(bar_free + 8 * b, (uint32_t)(((n >> 1) & 1) ^ 1), abortp)) {
-                        fail();
-                    } else {
-                        tc::fence_after_sync();
-#pragma unroll
-                        for (int tl = 0; tl < 2; tl++) {
-                            const uint64_t ad = tc::sw128_kmajor_desc(gP + (uint32_t)tl * TILE);
-#pragma unroll
-                            for (int k = 0; k < 4; k++)
-                                tc::mma_f16(tmem + T_D + (uint32_t)(b * 128 + tl * 64), ad + 2 * k,
-                                            bdesc + 2 * k, id_mma, k > 0);
-                        }
-                        tc::mma_commit(bar_mma1 + 8 * b);
-                        last_mma = n;
-                    }
-                }
-                if (u + 2 < nunits) {
-                    if (slot) pend1 = true;
-                    else pend0 = true;
-                }
+                tc::mbar_arrive(bar(BAR_EMPTY + slot));  // the ring slot may be refilled
+                tc::fence_proxy_async();                 // P is read by the tensor cores
+                tc::mbar_arrive(bar(BAR_PFULL + b));
             }
         }
-        // drain what is still in flight, bounded (copies only after an abort)
-        if (issuer) {
-            if (!ok) {
-                if (pend0) tc::mbar_wait(bar_in0, ph_in0);
-                if (pend1) tc::mbar_wait(bar_in1, ph_in1);
-            }
-            if (last_mma >= 0)
-                tc::mbar_wait(bar_mma1 + 8 * (uint32_t)(last_mma & 1), (uint32_t)((last_mma >> 1) & 1));
-        }
-    } else {
+    } else if (tid < PT + ET) {
         // ======================================================= epilogue role
-        // 16 warps: warp 8 + ew reads TMEM lane quarter qd = ew % 4 of tile
-        // tl = (ew / 4) % 2, columns [32 hc, 32 hc + 32) with hc = ew / 8.
+        // 16 warps.  Twiddle stage: warp 8 + ew reads TMEM lane quarter
+        // qd = ew % 4 of MMA 1 tile tl = (ew / 4) % 2, columns [32 hc, 32 hc + 32)
+        // with hc = ew / 8 (k1 in [16 hc, 16 hc + 16)).  Output stage: the same
+        // lane quarter of MMA 2's result, columns [32 cb, 32 cb + 32) with
+        // cb = ew / 4 (k1 mod 16 in [4 cb, 4 cb + 4), 8 spectra each).
         const int t = tid - PT, ew = t >> 5, l = t & 31;
         const uint32_t lane_q = (uint32_t)((ew & 3) * 32) << 16;
-        const int qd = ew & 3, tl = (ew >> 2) & 1, hc = ew >> 3;
-        const int su = tl * 4 + qd;  // spectrum of this thread's accumulator rows within the unit
-        const bool issuer = (t == 0);
-        const uint32_t gS = sbase + OFF_S;
-        const uint32_t stash = tmem + lane_q + T_STASH + (uint32_t)((ew >> 2) * 16);
-        long last_mma = -1;
+        const int qd = ew & 3, tl = (ew >> 2) & 1, hc = ew >> 3, cb = ew >> 2;
+        const int su = tl * 4 + qd;  // spectrum of this thread's MMA 1 rows within the unit
+        // MMA 2 row of this thread: (k2, re|im) for k1 in the lower (qd < 2) or upper half
+        const int k2 = (32 * (qd & 1) + l) >> 1, comp = l & 1;
+        const int k1base = 16 * (qd >> 1) + 4 * cb;
         bool ok = true;
         long n = 0;
         FJob a = L.one;
         int cur = -1;
-        auto sync_epi = [&]() { tc::named_barrier(2, ET); };
-        auto sync_epi_bad = [&]() { return tc::named_barrier_or(2, ET, bad); };
-
-        // Copy-out of a staged unit.  Units pair up into 16 spectra: the first
-        // unit's packed 16-byte re and im chunks wait in TMEM, the second writes
-        // both units' chunks as full 32-byte sectors (re chunks j, j+1 and im
-        // chunks 4+j, 5+j of a row are sector neighbours under the row swizzle).
-        bool have_prev = false;
-        auto copy_out = [&]() {
-            const OutUnit &o = prev_s;
-            const bool stash_only = !o.second && !o.lone;
-            const bool swap = (o.e & 1) != 0;  // the odd chunk comes first in the sector
-            // Lanes 2i and 2i+1 share a channel: lane 2i packs spectra 0-3 and
-            // writes the re sector, lane 2i+1 packs spectra 4-7 and writes the im
-            // sector, so each store instruction covers 16 rows (two sectors each)
-            // instead of 32.
-            const int hs = l & 1;
-            const uint32_t soff = hs ? (uint32_t)((((4 + o.j0) ^ (o.e & 7)) & ~1) << 4)
-                                     : (uint32_t)(((o.j0 ^ (o.e & 7)) & ~1) << 4);
-            const int nv = o.nvalid - 4 * hs;  // valid spectra of this lane's half
+        // the unit whose output is pending (its MMA 2 was issued last)
+        struct Pending {
+            uint8_t *X16;
+            int nep, nsp, e, sabs;
+        } pend{};
+        bool have_pend = false;
+        // output of unit m (MMA 2 result, converted and stored); false if a wait failed
+        auto output = [&](long m, const Pending &o) -> bool {
+            const int b = (int)(m & 1);
+            if (!wait_warp(bar(BAR_MMA2 + b), (uint32_t)((m >> 1) & 1))) return false;
+            tc::fence_after_sync();
+            uint32_t v[32];
+            const uint32_t tout = tmem + lane_q + T_D + (uint32_t)(b * 128 + 32 * cb);
+            tc::tmem_ld16(tout, *reinterpret_cast<uint32_t(*)[16]>(v));
+            tc::tmem_ld16(tout + 16, *reinterpret_cast<uint32_t(*)[16]>(v + 16));
+            tc::tmem_ld_wait();
+            tc::fence_before_sync();
+            tc::mbar_arrive(bar(BAR_DFREE + b));  // buffer b may take MMA 1 of unit m + 2
+            const int nvalid = o.nsp - o.sabs;     // valid spectra of the unit (>= 8: all)
+            const int j0 = (o.sabs & 31) >> 3;
+            if (nvalid < US) {
 #pragma unroll
-            for (int kp = 0; kp < 2; kp++) {
-                uint32_t p0[8];  // the first unit's chunks of rounds 2 kp, 2 kp + 1 (second unit only)
-                if (o.second) tc::tmem_ld8(stash + (uint32_t)(8 * kp), p0);
-                uint32_t q[8];  // this lane's 16-byte chunks of the unit, rounds 2 kp, 2 kp + 1
-#pragma unroll
-                for (int kr = 0; kr < 2; kr++) {
-                    const int c = (t >> 1) + 256 * (2 * kp + kr);
-                    uint32_t w[4];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const int sp = 4 * hs + i;
-                        w[i] = lds_u32(gS + (uint32_t)(c * 32) + (uint32_t)((sp ^ ((c >> 2) & 7)) << 2));
-                    }
-                    if (nv < 4) {
-#pragma unroll
-                        for (int i = 0; i < 4; i++)
-                            if (i >= nv) w[i] = 0u;
-                    }
-                    const uint32_t re0 = __byte_perm(w[0], w[1], 0x5410), re1 = __byte_perm(w[2], w[3], 0x5410);
-                    const uint32_t im0 = __byte_perm(w[0], w[1], 0x7632), im1 = __byte_perm(w[2], w[3], 0x7632);
-                    // lane 2i keeps re and sends im, lane 2i+1 keeps im and sends re
-                    const uint32_t x0 = __shfl_xor_sync(0xffffffffu, hs ? re0 : im0, 1);
-                    const uint32_t x1 = __shfl_xor_sync(0xffffffffu, hs ? re1 : im1, 1);
-                    q[4 * kr + 0] = hs ? x0 : re0;  // spectra 0-3, then 4-7, of this lane's component
-                    q[4 * kr + 1] = hs ? x1 : re1;
-                    q[4 * kr + 2] = hs ? im0 : x0;
-                    q[4 * kr + 3] = hs ? im1 : x1;
-                }
-                if (stash_only) {
-                    tc::tmem_st8(stash + (uint32_t)(8 * kp), q);
-                    continue;
-                }
-                if (o.second) tc::tmem_ld_wait();
-#pragma unroll
-                for (int kr = 0; kr < 2; kr++) {
-                    const int c = (t >> 1) + 256 * (2 * kp + kr);
-                    const uint32_t *fw = o.second ? p0 + 4 * kr : q + 4 * kr;  // first unit's chunk
-                    const uint4 f = make_uint4(fw[0], fw[1], fw[2], fw[3]);
-                    const uint4 sc = o.second ? make_uint4(q[4 * kr], q[4 * kr + 1], q[4 * kr + 2], q[4 * kr + 3])
-                                              : make_uint4(0u, 0u, 0u, 0u);
-                    uint8_t *row = o.X16 + (((size_t)o.kc * N + c) * o.nep + o.e) * 128;
-                    if (swap) stg32(row + soff, sc, f);
-                    else stg32(row + soff, f, sc);
-                }
+                for (int j = 0; j < 32; j++)
+                    if ((j & 7) >= nvalid) v[j] = 0u;
             }
-            if (stash_only) tc::tmem_st_wait();
+            // this unit's four 16-byte chunks (one per channel k1base + i)
+            uint32_t q[16];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float qs = MODE == OUT_Q8 ? qs_s[k1base + i + 32 * k2] : 1.0f;
+                const float *x = reinterpret_cast<const float *>(v + 8 * i);
+#pragma unroll
+                for (int h = 0; h < 4; h++) q[4 * i + h] = pack_out<MODE>(x[2 * h], x[2 * h + 1], qs);
+            }
+            // Units pair up into 16 spectra: chunks j and j + 1 of a component are
+            // neighbours in one 32-byte sector under the row swizzle, so the first
+            // unit of a pair parks its chunks in TMEM and the second writes both.
+            const bool second = (j0 & 1) != 0;
+            const bool last = nvalid <= US;  // the element's last unit
+            const uint32_t stash = tmem + lane_q + T_STASH + (uint32_t)(16 * cb);
+            if (!second && !last) {
+                tc::tmem_st16(stash, q);
+                tc::tmem_st_wait();
+                return true;
+            }
+            uint32_t f[16];
+            if (second) {
+                tc::tmem_ld16(stash, f);
+                tc::tmem_ld_wait();
+            }
+            const int jf = j0 & ~1;  // the pair's first chunk
+            const int xe = o.e & 7;
+            const uint32_t sec = (uint32_t)((((jf + 4 * comp) ^ xe) & ~1) << 4);
+            const bool swap = (xe & 1) != 0;  // the pair's second chunk comes first in the sector
+            const uint32_t zero4[4] = {0u, 0u, 0u, 0u};
+            const size_t rstride = (size_t)o.nep * 128;
+            uint8_t *row = o.X16 + ((size_t)((o.sabs >> 5) * N + k1base + 32 * k2) * o.nep + o.e) * 128;
+#pragma unroll
+            for (int i = 0; i < 4; i++, row += rstride) {
+                const uint32_t *c0 = second ? f + 4 * i : q + 4 * i;  // chunk jf
+                const uint32_t *c1 = second ? q + 4 * i : zero4;      // chunk jf + 1
+                if (swap) stg32(row + sec, c1, c0);
+                else stg32(row + sec, c0, c1);
+                if (last && jf == 0)  // zero the rest of the element's last 32-spectrum chunk
+                    stg32(row + (uint32_t)((((2 + 4 * comp) ^ xe) & ~1) << 4), zero4, zero4);
+            }
+            return true;
         };
-
         for (int w = blockIdx.x; w < L.nwork && ok; w += gridDim.x) {
             next_job(L, w, a, cur);
             const Item it = item_of(a, w);
             const int e = it.e, s0 = it.s0, nunits = it.nunits;
             for (int u = 0; u < nunits; u++, n++) {
                 const int b = (int)(n & 1);
-                const uint32_t tacc = tmem + lane_q + T_D + (uint32_t)(b * 128 + tl * 64 + 32 * hc);
-                // ---- twiddle: MMA 1 result (row = (spectrum, n2), col = k1) -> Z (row = (spectrum, k1), K = n2)
-                if (!wait_or_abort(bar_mma1 + 8 * b, (uint32_t)((n >> 1) & 1), abortp)) fail();
+                // ---- twiddle: MMA 1 result (row = (spectrum, n2), col = k1) -> Z in
+                //      operand buffer b, tile hc (row = 8 (k1 mod 16) + spectrum, K = n2)
+                if (!wait_warp(bar(BAR_MMA1 + b), (uint32_t)((n >> 1) & 1))) {
+                    fail();
+                    ok = false;
+                    break;
+                }
                 tc::fence_after_sync();
                 {
+                    const uint32_t tacc = tmem + lane_q + T_D + (uint32_t)(b * 128 + tl * 64 + 32 * hc);
                     uint32_t v[32];
                     tc::tmem_ld16(tacc, *reinterpret_cast<uint32_t(*)[16]>(v));
                     tc::tmem_ld16(tacc + 16, *reinterpret_cast<uint32_t(*)[16]>(v + 16));
                     tc::tmem_ld_wait();
-                    const uint32_t abase = gZ + (uint32_t)tl * TILE;
+                    const uint32_t zbase = sbase + OFF_P + (uint32_t)(b * 2 + hc) * TILE;
 #pragma unroll
                     for (int kk = 0; kk < 16; kk++) {
                         const int k1 = 16 * hc + kk;
@@ -615,68 +581,144 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                         const float2 tv = tw[k1 * 32 + l];
                         const float zr = fmaf(yr, tv.x, -yi * tv.y);
                         const float zi = fmaf(yr, tv.y, yi * tv.x);
-                        sts_u32(abase + tile_word(qd * 32 + k1, l), pack_h2<__half>(zr, zi));
+                        sts_u32(zbase + tile_word(8 * kk + su, l), pack_h2<__half>(zr, zi));
                     }
                 }
-                tc::fence_proxy_async();
-                tc::fence_before_sync();
-                if (sync_epi_bad()) {  // also orders the previous unit's staging before its copy-out
+                tc::fence_proxy_async();  // Z is read by the tensor cores
+                tc::fence_before_sync();  // MMA 2 overwrites the accumulators just read
+                tc::mbar_arrive(bar(BAR_ZFULL + b));
+                // ---- the previous unit's output while MMA 2 of this one runs
+                if (have_pend && !output(n - 1, pend)) {
+                    fail();
                     ok = false;
                     break;
                 }
-                if (issuer) {  // MMA 2 overwrites the accumulator buffer the twiddle stage has read
-                    tc::fence_after_sync();
-#pragma unroll
-                    for (int tt = 0; tt < 2; tt++) {
-                        const uint64_t ad = tc::sw128_kmajor_desc(gZ + (uint32_t)tt * TILE);
-#pragma unroll
-                        for (int k = 0; k < 4; k++)
-                            tc::mma_f16(tmem + T_D + (uint32_t)(b * 128 + tt * 64), ad + 2 * k, bdesc + 2 * k,
-                                        id_mma, k > 0);
-                    }
-                    tc::mma_commit(bar_mma2);
-                    last_mma = n;
-                }
-                // ---- the previous unit's copy-out runs while MMA 2 works
-                if (have_prev) copy_out();
-                // ---- output: MMA 2 result (row = (spectrum, k1), col = k2) -> staging S [channel][spectrum]
-                if (!wait_or_abort(bar_mma2, (uint32_t)(n & 1), abortp)) fail();
-                tc::fence_after_sync();
-                uint32_t v[32];
-                tc::tmem_ld16(tacc, *reinterpret_cast<uint32_t(*)[16]>(v));
-                tc::tmem_ld16(tacc + 16, *reinterpret_cast<uint32_t(*)[16]>(v + 16));
-                tc::tmem_ld_wait();
-                tc::fence_before_sync();
-                tc::mbar_arrive(bar_free + 8 * b);  // buffer b may take MMA 1 of unit n + 2
-                sync_epi();  // S is no longer read by the previous copy-out
-#pragma unroll
-                for (int kk = 0; kk < 16; kk++) {
-                    const int c = l + 32 * (16 * hc + kk);
-                    const float qs = MODE == OUT_Q8 ? qs_s[c] : 1.0f;
-                    sts_u32(gS + (uint32_t)(c * 32) + (uint32_t)((su ^ ((c >> 2) & 7)) << 2),
-                            pack_out<MODE>(__uint_as_float(v[2 * kk]), __uint_as_float(v[2 * kk + 1]), qs));
-                }
-                if (issuer) {  // read by every epilogue thread after the next barrier
-                    const int sabs = s0 + US * u;
-                    const bool second = (u & 1) != 0;
-                    const int s_first = second ? sabs - US : sabs;
-                    prev_s.X16 = a.X16;
-                    prev_s.nep = a.nep;
-                    prev_s.e = e;
-                    prev_s.kc = s_first >> 5;
-                    prev_s.j0 = (s_first & 31) >> 3;  // even
-                    prev_s.nvalid = min(US, a.nsp - sabs);
-                    prev_s.second = second;
-                    prev_s.lone = !second && u + 1 == nunits;  // first unit without a partner
-                }
-                have_prev = true;
+                pend = Pending{a.X16, a.nep, a.nsp, e, s0 + US * u};
+                have_pend = true;
             }
         }
-        if (ok && have_prev) {
-            sync_epi();  // the last unit's staging is complete
-            copy_out();
+        if (ok && have_pend && !output(n - 1, pend)) fail();
+    } else if (tid == PT + ET) {
+        // ========================================================= loader role
+        long total_uses = 0;  // this CTA's ring uses: one lead-in per work item, then its units
+        {
+            FJob a2 = L.one;
+            int c2 = -1;
+            for (int w = blockIdx.x; w < L.nwork; w += gridDim.x) {
+                next_job(L, w, a2, c2);
+                total_uses += 1 + item_of(a2, w).nunits;
+            }
         }
-        if (issuer && last_mma >= 0) tc::mbar_wait(bar_mma2, (uint32_t)(last_mma & 1));
+        FJob al = L.one;
+        int curl = -1, wl = blockIdx.x, ul = -1;  // ul = -1: the item's lead-in use
+        Item itl{};
+        const int nhist = L.table ? 0 : L.nhist;
+        auto row_src = [&](long rho, int e) -> const char2 * {
+            return rho < nhist ? L.hist + (rho * al.ne + e) * (long)N
+                               : al.iq + ((rho - nhist) * al.ne + e) * (long)N;
+        };
+        long rl = 0;  // next ring use to load
+        for (; rl < total_uses; rl++) {
+            const int slot = (int)(rl % NSLOT);
+            // the slot is free once the PFB has read use rl - NSLOT
+            if (rl >= NSLOT &&
+                !wait_or_abort(bar(BAR_EMPTY + slot), (uint32_t)(((rl / NSLOT) & 1) ^ 1), abortp)) {
+                fail();
+                break;
+            }
+            if (ul < 0) {
+                next_job(L, wl, al, curl);
+                itl = item_of(al, wl);
+            }
+            long r0;
+            int cnt;
+            if (ul < 0) {
+                r0 = itl.s0;
+                cnt = NT - 1;
+            } else {
+                r0 = itl.s0 + NT - 1 + US * ul;
+                const int rem = al.nsp - itl.s0 - US * ul;
+                cnt = rem < US ? rem : US;
+            }
+            const uint32_t full = bar(BAR_FULL + slot);
+            const uint32_t dst = gR + (uint32_t)(slot * US * ROWB);
+            tc::mbar_expect_tx(full, (uint32_t)(cnt * ROWB));
+            for (int q = 0; q < cnt; q++)
+                tc::bulk_g2s(dst + (uint32_t)(q * ROWB), row_src(r0 + q, itl.e), ROWB, full);
+            if (++ul == itl.nunits) {
+                ul = -1;
+                wl += gridDim.x;
+            }
+        }
+        // the copies issued are complete before the CTA ends (bounded waits)
+        for (long q = rl > NSLOT ? rl - NSLOT : 0; q < rl; q++)
+            tc::mbar_wait(bar(BAR_FULL + (int)(q % NSLOT)), (uint32_t)((q / NSLOT) & 1));
+    } else if (tid == PT + ET + 32) {
+        // ========================================================== MMA role
+        const uint32_t id_mma = tc::idesc_f16(64, 0, 0);    // MMA 1: M 128, N 64, f16 operands
+        const uint32_t id_mma2 = tc::idesc_f16(128, 0, 0);  // MMA 2: M 128, N 128
+        const uint64_t bdesc = tc::sw128_kmajor_desc(sbase + OFF_B);  // DFT rows 0-63
+        const uint64_t a2desc1 = tc::sw128_kmajor_desc(sbase + OFF_B2);
+        long total_units = 0;
+        {
+            FJob a2 = L.one;
+            int c2 = -1;
+            for (int w = blockIdx.x; w < L.nwork; w += gridDim.x) {
+                next_job(L, w, a2, c2);
+                total_units += item_of(a2, w).nunits;
+            }
+        }
+        long n1 = 0, n2 = 0;  // next MMA 1 and MMA 2 unit
+        long long t_last = clock64();
+        while (n2 < total_units) {
+            if (*abortp) break;
+            bool progress = false;
+            if (n2 < n1 &&
+                tc::mbar_test_wait(bar(BAR_ZFULL + (int)(n2 & 1)), (uint32_t)((n2 >> 1) & 1))) {
+                tc::fence_after_sync();
+                const int b = (int)(n2 & 1);
+                const uint32_t dcol = tmem + T_D + (uint32_t)(b * 128);
+                const uint32_t gz = sbase + OFF_P + (uint32_t)b * 2 * TILE;
+                const uint64_t z0 = tc::sw128_kmajor_desc(gz), z1 = tc::sw128_kmajor_desc(gz + TILE);
+#pragma unroll
+                for (int k = 0; k < 4; k++) tc::mma_f16(dcol, bdesc + 2 * k, z0 + 2 * k, id_mma2, k > 0);
+#pragma unroll
+                for (int k = 0; k < 4; k++) tc::mma_f16(dcol, a2desc1 + 2 * k, z1 + 2 * k, id_mma2, 1);
+                tc::mma_commit(bar(BAR_MMA2 + b));   // the accumulators are readable
+                tc::mma_commit(bar(BAR_PFREE + b));  // the operand buffer may take P again
+                n2++;
+                progress = true;
+            }
+            if (n1 < total_units) {
+                const int b = (int)(n1 & 1);
+                if (tc::mbar_test_wait(bar(BAR_PFULL + b), (uint32_t)((n1 >> 1) & 1)) &&
+                    (n1 < 2 || tc::mbar_test_wait(bar(BAR_DFREE + b), (uint32_t)(((n1 >> 1) & 1) ^ 1)))) {
+                    tc::fence_after_sync();
+                    const uint32_t gP = sbase + OFF_P + (uint32_t)b * 2 * TILE;
+#pragma unroll
+                    for (int tt = 0; tt < 2; tt++) {
+                        const uint64_t ad = tc::sw128_kmajor_desc(gP + (uint32_t)tt * TILE);
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            tc::mma_f16(tmem + T_D + (uint32_t)(b * 128 + tt * 64), ad + 2 * k,
+                                        bdesc + 2 * k, id_mma, k > 0);
+                    }
+                    tc::mma_commit(bar(BAR_MMA1 + b));
+                    n1++;
+                    progress = true;
+                }
+            }
+            if (progress) {
+                t_last = clock64();
+            } else if (clock64() - t_last > tc::kWaitCycles) {
+                fail();
+                break;
+            }
+        }
+        // the products issued are complete before the CTA frees its tensor memory
+        if (n1 > 0) tc::mbar_wait(bar(BAR_MMA1 + (int)((n1 - 1) & 1)), (uint32_t)(((n1 - 1) >> 1) & 1));
+        if (n2 > 0)
+            tc::mbar_wait(bar(BAR_MMA2 + (int)((n2 - 1) & 1)), (uint32_t)(((n2 - 1) >> 1) & 1));
     }
     tc::fence_before_sync();
     __syncthreads();
