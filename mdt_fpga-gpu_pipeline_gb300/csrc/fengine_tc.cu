@@ -60,9 +60,11 @@ constexpr uint32_t SMEM = OFF_RING + NSLOT * US * ROWB;
 // writes buffer u % 2 as two 64-column tiles, MMA 2 of the same unit
 // overwrites all 128 columns once the twiddle stage has read them), the
 // packed output chunks of the first unit of each pair of 8-spectrum units
-// (16 columns per epilogue thread), and the PFB carry: per PFB thread and
-// channel the last Ntaps-1 converted input rows (16 columns).
-constexpr uint32_t TMEM_COLS = 512, T_D = 0, T_STASH = 256, T_CARRY = 320;
+// (16 columns per epilogue thread), the PFB carry: per PFB thread and
+// channel the last Ntaps-1 converted input rows (16 columns), and the
+// twiddles w_1024^{n2 k1} of the epilogue's twiddle stage (lane n2 of each
+// lane quarter, 32 columns per half of the k1 range).
+constexpr uint32_t TMEM_COLS = 512, T_D = 0, T_STASH = 256, T_CARRY = 320, T_TW = 448;
 // mbarriers (per ring slot, or per operand / accumulator buffer, so that no
 // waiter is ever more than one phase behind): ring slot filled (bulk copies
 // landed) / emptied (PFB has read it); P written; MMA 1 done; Z written;
@@ -481,6 +483,26 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
         // MMA 2 row of this thread: (k2, re|im) for k1 in the lower (qd < 2) or upper half
         const int k2 = (32 * (qd & 1) + l) >> 1, comp = l & 1;
         const int k1base = 16 * (qd >> 1) + 4 * cb;
+        // twiddles of this thread's twiddle stage (k1 in [16 hc, 16 hc + 16), n2 = l) in
+        // TMEM columns T_TW + 32 hc of its lane quarter, written once by the tl = 0 warps
+        const uint32_t ttw = tmem + lane_q + T_TW + (uint32_t)(32 * hc);
+        if (tl == 0) {
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                uint32_t tv[16];
+#pragma unroll
+                for (int kk = 0; kk < 8; kk++) {
+                    const float2 w = tw[(16 * hc + 8 * hh + kk) * 32 + l];
+                    tv[2 * kk] = __float_as_uint(w.x);
+                    tv[2 * kk + 1] = __float_as_uint(w.y);
+                }
+                tc::tmem_st16(ttw + (uint32_t)(16 * hh), tv);
+            }
+            tc::tmem_st_wait();
+        }
+        tc::fence_before_sync();
+        tc::named_barrier(2, ET);
+        tc::fence_after_sync();
         bool ok = true;
         long n = 0;
         FJob a = L.one;
@@ -575,13 +597,19 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     tc::tmem_ld_wait();
                     const uint32_t zbase = sbase + OFF_P + (uint32_t)(b * 2 + hc) * TILE;
 #pragma unroll
-                    for (int kk = 0; kk < 16; kk++) {
-                        const int k1 = 16 * hc + kk;
-                        const float yr = __uint_as_float(v[2 * kk]), yi = __uint_as_float(v[2 * kk + 1]);
-                        const float2 tv = tw[k1 * 32 + l];
-                        const float zr = fmaf(yr, tv.x, -yi * tv.y);
-                        const float zi = fmaf(yr, tv.y, yi * tv.x);
-                        sts_u32(zbase + tile_word(8 * kk + su, l), pack_h2<__half>(zr, zi));
+                    for (int hh = 0; hh < 2; hh++) {
+                        uint32_t tv[16];
+                        tc::tmem_ld16(ttw + (uint32_t)(16 * hh), tv);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int k = 0; k < 8; k++) {
+                            const int kk = 8 * hh + k;
+                            const float yr = __uint_as_float(v[2 * kk]), yi = __uint_as_float(v[2 * kk + 1]);
+                            const float tr = __uint_as_float(tv[2 * k]), ti = __uint_as_float(tv[2 * k + 1]);
+                            const float zr = fmaf(yr, tr, -yi * ti);
+                            const float zi = fmaf(yr, ti, yi * tr);
+                            sts_u32(zbase + tile_word(8 * kk + su, l), pack_h2<__half>(zr, zi));
+                        }
                     }
                 }
                 tc::fence_proxy_async();  // Z is read by the tensor cores
