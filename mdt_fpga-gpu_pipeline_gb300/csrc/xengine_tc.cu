@@ -17,6 +17,10 @@
 // K=16 MMAs on two accumulators (k-steps 0,1 = re, 2,3 = im):
 //     Re V += A0 B0 + A1 B1 + A2 B2 + A3 B3
 //     Im V += A2 B0 + A3 B1 - A0 B2 - A1 B3        (negate-A bit)
+// On a diagonal tile (rows and columns are the same elements, A = B) the
+// imaginary part is antisymmetric: Im V = G - G^T with G = X_im X_re^T, so
+// only G += A2 B0 + A3 B1 is accumulated (six MMAs instead of eight) and the
+// epilogue forms G[r][q] - G[q][r] through shared memory.
 // A block owns one (channel, row tile of 128 elements, column chunk of up to
 // 256 elements) of the lower triangle: only tiles on or below the diagonal
 // are computed; the epilogue writes the lower triangle and its conjugate
@@ -55,14 +59,31 @@ constexpr int TC_THREADS = 192;
 // block (producer, MMA, 16 epilogue warps holding the int32 running sums)
 constexpr int tc_threads(int kind) { return kind == 1 ? 576 : TC_THREADS; }
 constexpr int TC_MAX_TILES = 160;
-constexpr uint32_t TC_B_BYTES = TC_BROWS * 128;
 constexpr uint32_t TC_A_BYTES = TC_AROWS * 128;
-constexpr uint32_t TC_STAGE_BYTES = TC_B_BYTES + TC_A_BYTES;
-constexpr size_t TC_SMEM = 1024 /*align slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES + 256;
-// shared memory of the single-launch kernel for a (BROWS, STAGES) shape
-constexpr size_t tc_smem(int brows, int stages)
+// Epilogue scratch of the f16/bf16 kernel with 128-wide chunks, reused from the
+// stage ring once every MMA has completed: the per-warp 32 x 33 transpose
+// blocks of the conjugate mirror, then a diagonal tile's G (128 rows of 129
+// floats, the odd stride keeping row and column accesses conflict-free).
+constexpr int TC_GS = 129;
+constexpr size_t TC_TB_BYTES = 4 * 32 * 33 * sizeof(float2);
+constexpr size_t TC_GS_BYTES = (size_t)TC_AROWS * TC_GS * sizeof(float);
+constexpr bool tc_sym(int kind, int brows) { return kind == 0 && brows == 128; }
+// the batched kernel's stage (B chunks of <= TCB_MAXW rows, then A) and shared memory
+constexpr uint32_t TCB_B_BYTES = TCB_MAXW * 128;
+constexpr uint32_t TCB_STAGE_BYTES = TCB_B_BYTES + TC_A_BYTES;
+constexpr size_t TCB_SMEM = 1024 + (size_t)TC_STAGES * TCB_STAGE_BYTES + TC_GS_BYTES + 256;
+// offset of the mbarriers: after the stage ring and after the epilogue scratch
+constexpr size_t tc_bar_off(int kind, int brows, int stages)
 {
-    return 1024 + (size_t)stages * ((size_t)brows * 128 + TC_A_BYTES) + 256;
+    return tc_sym(kind, brows) &&
+                   TC_TB_BYTES + TC_GS_BYTES > (size_t)stages * ((size_t)brows * 128 + TC_A_BYTES)
+               ? TC_TB_BYTES + TC_GS_BYTES
+               : (size_t)stages * ((size_t)brows * 128 + TC_A_BYTES);
+}
+// shared memory of the single-launch kernel for a (KIND, BROWS, STAGES) shape
+constexpr size_t tc_smem(int kind, int brows, int stages)
+{
+    return 1024 + tc_bar_off(kind, brows, stages) + 256;
 }
 
 
@@ -96,7 +117,7 @@ __global__ void __launch_bounds__(tc_threads(KIND), (KIND == 0 && BROWS == 128 ?
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *bars = (uint64_t *)(smem + (size_t)STAGES * STAGE_BYTES);
+    uint64_t *bars = (uint64_t *)(smem + tc_bar_off(KIND, BROWS, STAGES));
     // bars[0..S) full, bars[S..2S) empty, bars[2S] done, bars[2S+1..2S+2] window
     // full, bars[2S+3..2S+4] window empty; then the TMEM address slot
     uint64_t *win_full = bars + 2 * STAGES + 1;
@@ -107,6 +128,8 @@ __global__ void __launch_bounds__(tc_threads(KIND), (KIND == 0 && BROWS == 128 ?
     const int ch = blockIdx.x / a.ntiles;
     const TcTile tile = a.tiles[blockIdx.x - ch * a.ntiles];
     const int N = tile.n;
+    // diagonal tile: rows and columns are the same elements (A read from B's rows)
+    const bool sym = tc_sym(KIND, BROWS) && tile.r0 == tile.q0 && !tile.a_sep;
     constexpr int NCOLMUL = (KIND == 0) ? 2 : 4;  // TMEM columns per output column
     const uint32_t ncols = (NCOLMUL * N <= 32) ? 32 : (NCOLMUL * N <= 64) ? 64
                          : (NCOLMUL * N <= 128) ? 128 : (NCOLMUL * N <= 256) ? 256 : 512;
@@ -191,8 +214,10 @@ __global__ void __launch_bounds__(tc_threads(KIND), (KIND == 0 && BROWS == 128 ?
             tc::mma_f16(acc_re, ad + 6, bd + 6, id_pos, 1);
             tc::mma_f16(acc_im, ad + 4, bd + 0, id_pos, !first);
             tc::mma_f16(acc_im, ad + 6, bd + 2, id_pos, 1);
-            tc::mma_f16(acc_im, ad + 0, bd + 4, id_neg, 1);
-            tc::mma_f16(acc_im, ad + 2, bd + 6, id_neg, 1);
+            if (!sym) {  // a diagonal tile's Im is G - G^T, formed in the epilogue
+                tc::mma_f16(acc_im, ad + 0, bd + 4, id_neg, 1);
+                tc::mma_f16(acc_im, ad + 2, bd + 6, id_neg, 1);
+            }
             tc::mma_commit(tc::smem_u32(&bars[STAGES + s]));
             if constexpr (KIND == 1) {
                 if ((kc % TC_WIN) == TC_WIN - 1 || kc == a.nkc - 1)
@@ -284,6 +309,21 @@ __global__ void __launch_bounds__(tc_threads(KIND), (KIND == 0 && BROWS == 128 ?
         // so that it is written along q as well.
         float2 *tb = reinterpret_cast<float2 *>(smem) + (size_t)quarter * 32 * 33;  // [q][r]
         const int rbase = tile.r0 + quarter * 32;
+        // diagonal tile: G (the Im accumulator) row by row into shared memory, so
+        // that each thread can read the transposed entry G[q][r] (tile-local)
+        float *gs = reinterpret_cast<float *>(smem + TC_TB_BYTES);
+        const int rl = quarter * 32 + lane;
+        if (sym) {
+            for (int n0 = 0; n0 < N; n0 += 16) {
+                uint32_t vg[16];
+                tc::tmem_ld16(d_im + lane_off + n0, vg);
+                tc::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (n0 + j < N) gs[rl * TC_GS + n0 + j] = __uint_as_float(vg[j]);
+            }
+        }
+        if (tc_sym(KIND, BROWS)) tc::named_barrier(1, 128);  // the four epilogue warps
         for (int n0 = 0; n0 < N; n0 += 32) {
 #pragma unroll
             for (int h = 0; h < 2; h++) {
@@ -299,7 +339,8 @@ __global__ void __launch_bounds__(tc_threads(KIND), (KIND == 0 && BROWS == 128 ?
                     const int q = tile.q0 + n0 + 16 * h + j;
                     const bool live = has && ok && r < a.ne && q < a.ne && q <= r;
                     const float re = live ? __uint_as_float(vr[j]) * a.alpha : 0.0f;
-                    const float im = (live && q != r) ? __uint_as_float(vi[j]) * a.alpha : 0.0f;
+                    const float g = sym && live ? gs[(n0 + 16 * h + j) * TC_GS + rl] : 0.0f;
+                    const float im = (live && q != r) ? (__uint_as_float(vi[j]) - g) * a.alpha : 0.0f;
                     tb[(16 * h + j) * 33 + lane] = make_float2(re, -im);
                     if (!live) continue;
                     const long lo = (long)q * a.ne + r;
@@ -351,7 +392,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *bars = (uint64_t *)(smem + (size_t)TC_STAGES * TC_STAGE_BYTES);
+    // stage ring, then a diagonal entry's G (128 x TC_GS floats), then the barriers
+    float *gs = reinterpret_cast<float *>(smem + (size_t)TC_STAGES * TCB_STAGE_BYTES);
+    uint64_t *bars = (uint64_t *)(smem + (size_t)TC_STAGES * TCB_STAGE_BYTES + TC_GS_BYTES);
     uint64_t *acc_full = bars + 2 * TC_STAGES, *acc_empty = bars + 2 * TC_STAGES + 2;
     uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 4);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -388,13 +431,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                        (uint32_t)((it / TC_STAGES) - 1) & 1);
                     if (!ok) break;
                 }
-                uint8_t *stage = smem + (size_t)s * TC_STAGE_BYTES;
+                uint8_t *stage = smem + (size_t)s * TCB_STAGE_BYTES;
                 const uint32_t full = tc::smem_u32(&bars[s]);
                 tc::mbar_expect_tx(full, bbytes + abytes);
                 const uint8_t *src = xc + (long)kc * jb.chunk_bytes;
                 tc::bulk_g2s(tc::smem_u32(stage), src + (long)wk.tile.q0 * 128, bbytes, full);
                 if (abytes)
-                    tc::bulk_g2s(tc::smem_u32(stage + TC_B_BYTES), src + (long)wk.tile.r0 * 128,
+                    tc::bulk_g2s(tc::smem_u32(stage + TCB_B_BYTES), src + (long)wk.tile.r0 * 128,
                                  abytes, full);
             }
         }
@@ -410,6 +453,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const XWork wk = work[w];
             const XJob jb = jobs[wk.job];
             const int N = wk.tile.n, h = t & 1;
+            // diagonal entry (A read from B's rows): Im = G - G^T in the epilogue
+            const bool sym = wk.tile.r0 == wk.tile.q0 && !wk.tile.a_sep;
             if (t >= 2) {
                 ok = tc::mbar_wait(tc::smem_u32(&acc_empty[h]), ((t >> 1) - 1) & 1);
                 if (!ok) break;
@@ -422,8 +467,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 ok = tc::mbar_wait(tc::smem_u32(&bars[s]), (uint32_t)(it / TC_STAGES) & 1);
                 if (!ok) break;
                 tc::fence_after_sync();
-                const uint32_t sb = tc::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
-                const uint32_t sa = wk.tile.a_sep ? sb + TC_B_BYTES
+                const uint32_t sb = tc::smem_u32(smem + (size_t)s * TCB_STAGE_BYTES);
+                const uint32_t sa = wk.tile.a_sep ? sb + TCB_B_BYTES
                                                   : sb + (uint32_t)(wk.tile.r0 - wk.tile.q0) * 128;
                 const uint64_t bd = tc::sw128_kmajor_desc(sb), ad = tc::sw128_kmajor_desc(sa);
                 const uint32_t acc = kc > 0;
@@ -433,8 +478,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 tc::mma_f16(d_re, ad + 6, bd + 6, id_pos, 1);
                 tc::mma_f16(d_im, ad + 4, bd + 0, id_pos, acc);
                 tc::mma_f16(d_im, ad + 6, bd + 2, id_pos, 1);
-                tc::mma_f16(d_im, ad + 0, bd + 4, id_neg, 1);
-                tc::mma_f16(d_im, ad + 2, bd + 6, id_neg, 1);
+                if (!sym) {
+                    tc::mma_f16(d_im, ad + 0, bd + 4, id_neg, 1);
+                    tc::mma_f16(d_im, ad + 2, bd + 6, id_neg, 1);
+                }
                 tc::mma_commit(tc::smem_u32(&bars[TC_STAGES + s]));
             }
             tc::mma_commit(tc::smem_u32(&acc_full[h]));
@@ -448,10 +495,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const XWork wk = work[w];
             const XJob jb = jobs[wk.job];
             const int N = wk.tile.n, h = t & 1;
+            const bool sym = wk.tile.r0 == wk.tile.q0 && !wk.tile.a_sep;
             ok = ok && tc::mbar_wait_sleep(tc::smem_u32(&acc_full[h]), (t >> 1) & 1);
+            // the four epilogue warps agree on ok (so that they leave together and
+            // meet at every barrier below) and have finished the previous entry's
+            // reads of gs
+            ok = !tc::named_barrier_or(1, 128, !ok);
             tc::fence_after_sync();
             const uint32_t d_re = tmem + (uint32_t)(h * 256), d_im = d_re + (uint32_t)N;
-            const int r = wk.tile.r0 + quarter * 32 + lane;
+            const int rl = quarter * 32 + lane;
+            const int r = wk.tile.r0 + rl;
+            if (sym) {  // G row by row into shared memory, for the transposed entries
+                for (int n0 = 0; n0 < N; n0 += 16) {
+                    uint32_t vg[16];
+                    tc::tmem_ld16(d_im + lane_off + n0, vg);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (n0 + j < N) gs[rl * TC_GS + n0 + j] = __uint_as_float(vg[j]);
+                }
+                tc::named_barrier(1, 128);
+            }
             // no visibility buffer (autotuning before the first execute): no writes
             float2 *Vc = jb.V ? jb.V + (long)wk.ch * jb.ne * jb.ne : nullptr;
             for (int n0 = 0; n0 < N; n0 += 16) {
@@ -465,7 +529,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const int q = wk.tile.q0 + n0 + j;
                     if (q >= jb.ne || q > r) continue;
                     const float re = __uint_as_float(vr[j]) * jb.alpha;
-                    const float im = (q == r) ? 0.0f : __uint_as_float(vi[j]) * jb.alpha;
+                    const float g = sym ? gs[(n0 + j) * TC_GS + rl] : 0.0f;
+                    const float im = (q == r) ? 0.0f : (__uint_as_float(vi[j]) - g) * jb.alpha;
                     Vc[(long)q * jb.ne + r] = make_float2(re, im);
                     if (q != r) Vc[(long)r * jb.ne + q] = make_float2(re, -im);
                 }
@@ -489,23 +554,26 @@ mdt_status xengine_tc_batched(const XJob *jobs, const XWork *work, int nwork, in
 {
     if (nwork <= 0) return MDT_SUCCESS;
     cudaError_t e = cudaFuncSetAttribute(xengine_tc_batched_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TCB_SMEM);
     if (e != cudaSuccess) return cuda_status(e, "batched X-engine smem attribute");
     const int blocks = std::min(nwork, sm_count());
-    xengine_tc_batched_kernel<<<blocks, TC_THREADS, TC_SMEM, stream>>>(jobs, work, nwork, err);
+    xengine_tc_batched_kernel<<<blocks, TC_THREADS, TCB_SMEM, stream>>>(jobs, work, nwork, err);
     return launch_status("xengine_tc_batched_kernel");
 }
 
 // Lower-triangle work list for NE elements: row tiles of 128, column chunks
-// of up to 256 from 0 to the end of the row tile's diagonal block.
+// of up to maxw from 0 to the end of the row tile's diagonal block.
 int make_tiles(int ne, int nep, int maxw, TcTile *tiles)
 {
     int n = 0;
     for (int r0 = 0; r0 < nep; r0 += TC_AROWS) {
         const int cend = std::min(nep, r0 + TC_AROWS);
-        for (int q0 = 0; q0 < cend; q0 += maxw) {
+        for (int q0 = 0; q0 < cend;) {
             if (n >= TC_MAX_TILES) return -1;
-            const int w = std::min(maxw, cend - q0);
+            // Chunks narrower than the row tile leave the diagonal block whole:
+            // its chunk holds every row of the tile, so that A is read from B's
+            // rows and the imaginary part is formed as G - G^T.
+            const int w = (maxw < TC_AROWS && q0 == r0) ? cend - q0 : std::min(maxw, cend - q0);
             TcTile t;
             t.r0 = (int16_t)r0;
             t.q0 = (int16_t)q0;
@@ -518,6 +586,7 @@ int make_tiles(int ne, int nep, int maxw, TcTile *tiles)
                                 r0 - q0 + TC_AROWS <= TC_BROWS;
             t.a_sep = (int16_t)(inside ? 0 : 1);
             tiles[n++] = t;
+            q0 += w;
         }
     }
     return n;
@@ -563,8 +632,8 @@ mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, flo
         kern<<<(unsigned)blocks, TC_THREADS, smem, stream>>>(a);
         return launch_status("xengine_tc_kernel");
     };
-    return wide ? launch(xengine_tc_kernel<0, 256, 4>, tc_smem(256, 4))
-                : launch(xengine_tc_kernel<0, 128, 3>, tc_smem(128, 3));
+    return wide ? launch(xengine_tc_kernel<0, 256, 4>, tc_smem(0, 256, 4))
+                : launch(xengine_tc_kernel<0, 128, 3>, tc_smem(0, 128, 3));
 }
 
 // Exact int8 mode: X16 holds integers in [-127, 127] (f16) requantised with
@@ -593,11 +662,11 @@ mdt_status xengine_q8(int ne, int nch, int nsp, const void *X16, const float *qs
     if (a.ntiles <= 0) return invalid("xengine_q8: too many tiles");
     cudaError_t e = cudaFuncSetAttribute(xengine_tc_kernel<1, 128, 4>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)tc_smem(128, 4));
+                                         (int)tc_smem(1, 128, 4));
     if (e != cudaSuccess) return cuda_status(e, "xengine_q8 smem attribute");
     long blocks = (long)nch * a.ntiles;
     if (blocks > 0x7fffffffL) return invalid("xengine_q8: grid too large");
-    xengine_tc_kernel<1, 128, 4><<<(unsigned)blocks, tc_threads(1), tc_smem(128, 4), stream>>>(a);
+    xengine_tc_kernel<1, 128, 4><<<(unsigned)blocks, tc_threads(1), tc_smem(1, 128, 4), stream>>>(a);
     return launch_status("xengine_tc_kernel<exact int8>");
 }
 
