@@ -270,10 +270,10 @@ __device__ __forceinline__ Item item_of(const FJob &a, int w)
 // mbarriers (no named barrier between warps):
 //  * loader (warp 24, one thread): the bulk copies of the input rows into an
 //    NSLOT-slot ring, up to NSLOT uses ahead of the PFB;
-//  * MMA issuer (warp 25, one thread): MMA 2 of each unit once its Z tiles
-//    are written (first, the epilogue waits on it), MMA 1 once its P tiles
-//    are written and its accumulator buffer is free; it polls both
-//    conditions without blocking on either;
+//  * MMA issuer (warp 25, one thread): in a fixed order, MMA 2 of unit k
+//    once its Z tiles are written, then MMA 1 of unit k + 1 once its P tiles
+//    are written and its accumulator buffer is free, each as soon as its
+//    mbarriers complete (the waiting thread is suspended, not polling);
 //  * PFB (warps 0-7): per ring use, either a work item's Ntaps-1 lead-in rows
 //    into the tap carry (TMEM) or one unit's tap sum into operand buffer
 //    u % 2, once MMA 2 of unit u - 2 has read that buffer;
@@ -696,53 +696,67 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                 total_units += item_of(a2, w).nunits;
             }
         }
-        long n1 = 0, n2 = 0;  // next MMA 1 and MMA 2 unit
-        long long t_last = clock64();
-        while (n2 < total_units) {
-            if (*abortp) break;
-            bool progress = false;
-            if (n2 < n1 &&
-                tc::mbar_test_wait(bar(BAR_ZFULL + (int)(n2 & 1)), (uint32_t)((n2 >> 1) & 1))) {
+        // MMA 1 of unit u: accumulator buffer u % 2 <- P tiles x DFT
+        auto issue_mma1 = [&](long u) {
+            const int b = (int)(u & 1);
+            const uint32_t gP = sbase + OFF_P + (uint32_t)b * 2 * TILE;
+#pragma unroll
+            for (int tt = 0; tt < 2; tt++) {
+                const uint64_t ad = tc::sw128_kmajor_desc(gP + (uint32_t)tt * TILE);
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    tc::mma_f16(tmem + T_D + (uint32_t)(b * 128 + tt * 64), ad + 2 * k,
+                                bdesc + 2 * k, id_mma, k > 0);
+            }
+            tc::mma_commit(bar(BAR_MMA1 + b));
+        };
+        // MMA 2 of unit u: accumulator buffer u % 2 <- blockdiag(DFT, DFT) x Z^T
+        auto issue_mma2 = [&](long u) {
+            const int b = (int)(u & 1);
+            const uint32_t dcol = tmem + T_D + (uint32_t)(b * 128);
+            const uint32_t gz = sbase + OFF_P + (uint32_t)b * 2 * TILE;
+            const uint64_t z0 = tc::sw128_kmajor_desc(gz), z1 = tc::sw128_kmajor_desc(gz + TILE);
+#pragma unroll
+            for (int k = 0; k < 4; k++) tc::mma_f16(dcol, bdesc + 2 * k, z0 + 2 * k, id_mma2, k > 0);
+#pragma unroll
+            for (int k = 0; k < 4; k++) tc::mma_f16(dcol, a2desc1 + 2 * k, z1 + 2 * k, id_mma2, 1);
+            tc::mma_commit(bar(BAR_MMA2 + b));   // the accumulators are readable
+            tc::mma_commit(bar(BAR_PFREE + b));  // the operand buffer may take P again
+        };
+        // Fixed order, each step issued as soon as its inputs are ready (blocking,
+        // bounded waits): MMA 1 of unit 0, then per unit k, MMA 2 of k once its Z
+        // tiles are written, and MMA 1 of k + 1 once its P tiles are written and
+        // its accumulator buffer is free (the epilogue has read MMA 2 of k - 1).
+        // In the epilogue's order these events come as Z(k), then the read of
+        // MMA 2 of k - 1, so no step waits on a later one.
+        long n1 = 0, n2 = 0;  // MMA 1 and MMA 2 units issued
+        bool okm = true;
+        if (total_units > 0) {
+            okm = wait_or_abort(bar(BAR_PFULL), 0u, abortp);
+            if (okm) {
                 tc::fence_after_sync();
-                const int b = (int)(n2 & 1);
-                const uint32_t dcol = tmem + T_D + (uint32_t)(b * 128);
-                const uint32_t gz = sbase + OFF_P + (uint32_t)b * 2 * TILE;
-                const uint64_t z0 = tc::sw128_kmajor_desc(gz), z1 = tc::sw128_kmajor_desc(gz + TILE);
-#pragma unroll
-                for (int k = 0; k < 4; k++) tc::mma_f16(dcol, bdesc + 2 * k, z0 + 2 * k, id_mma2, k > 0);
-#pragma unroll
-                for (int k = 0; k < 4; k++) tc::mma_f16(dcol, a2desc1 + 2 * k, z1 + 2 * k, id_mma2, 1);
-                tc::mma_commit(bar(BAR_MMA2 + b));   // the accumulators are readable
-                tc::mma_commit(bar(BAR_PFREE + b));  // the operand buffer may take P again
-                n2++;
-                progress = true;
-            }
-            if (n1 < total_units) {
-                const int b = (int)(n1 & 1);
-                if (tc::mbar_test_wait(bar(BAR_PFULL + b), (uint32_t)((n1 >> 1) & 1)) &&
-                    (n1 < 2 || tc::mbar_test_wait(bar(BAR_DFREE + b), (uint32_t)(((n1 >> 1) & 1) ^ 1)))) {
-                    tc::fence_after_sync();
-                    const uint32_t gP = sbase + OFF_P + (uint32_t)b * 2 * TILE;
-#pragma unroll
-                    for (int tt = 0; tt < 2; tt++) {
-                        const uint64_t ad = tc::sw128_kmajor_desc(gP + (uint32_t)tt * TILE);
-#pragma unroll
-                        for (int k = 0; k < 4; k++)
-                            tc::mma_f16(tmem + T_D + (uint32_t)(b * 128 + tt * 64), ad + 2 * k,
-                                        bdesc + 2 * k, id_mma, k > 0);
-                    }
-                    tc::mma_commit(bar(BAR_MMA1 + b));
-                    n1++;
-                    progress = true;
-                }
-            }
-            if (progress) {
-                t_last = clock64();
-            } else if (clock64() - t_last > tc::kWaitCycles) {
-                fail();
-                break;
+                issue_mma1(0);
+                n1 = 1;
             }
         }
+        for (long k = 0; okm && k < total_units; k++) {
+            okm = wait_or_abort(bar(BAR_ZFULL + (int)(k & 1)), (uint32_t)((k >> 1) & 1), abortp);
+            if (!okm) break;
+            tc::fence_after_sync();
+            issue_mma2(k);
+            n2 = k + 1;
+            const long u = k + 1;
+            if (u < total_units) {
+                const int b = (int)(u & 1);
+                okm = wait_or_abort(bar(BAR_PFULL + b), (uint32_t)((u >> 1) & 1), abortp) &&
+                      (u < 2 || wait_or_abort(bar(BAR_DFREE + b), (uint32_t)(((u >> 1) & 1) ^ 1), abortp));
+                if (!okm) break;
+                tc::fence_after_sync();
+                issue_mma1(u);
+                n1 = u + 1;
+            }
+        }
+        if (!okm) fail();
         // the products issued are complete before the CTA frees its tensor memory
         if (n1 > 0) tc::mbar_wait(bar(BAR_MMA1 + (int)((n1 - 1) & 1)), (uint32_t)(((n1 - 1) >> 1) & 1));
         if (n2 > 0)
