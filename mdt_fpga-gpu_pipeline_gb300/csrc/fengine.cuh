@@ -16,8 +16,8 @@ struct FJob {
     int wk0;           // first work item of the job in a tensor-core F-engine launch
 };
 
-// Work items of one job in a tensor-core F-engine launch (runs of 256 spectra).
-inline long fjob_tc_items(int ne, int nsp) { return (long)ne * ((nsp + 255) / 256); }
+// Work items of one job in a tensor-core F-engine launch (runs of 512 spectra).
+inline long fjob_tc_items(int ne, int nsp) { return (long)ne * ((nsp + 511) / 512); }
 // Whether the tensor-core F-engine handles this shape.
 inline bool fengine_tc_shape(int nch, int ntaps) { return nch == 1024 && (ntaps == 4 || ntaps == 8); }
 

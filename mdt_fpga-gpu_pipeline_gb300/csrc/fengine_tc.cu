@@ -44,7 +44,7 @@ constexpr int NSLOT = 4;                // input ring slots
 constexpr int US = 8;                   // spectra per unit
 constexpr int CPT = N / PT;             // channels per PFB thread
 constexpr int ROWB = 2 * N;             // one (spectrum, element) row of int8 I/Q
-constexpr int RUN = 256;                // spectra per work item
+constexpr int RUN = 512;                // spectra per work item
 constexpr uint32_t TILE = 16384;        // 128 rows x 128 bytes
 // shared memory: the 128 x 128 block-diagonal DFT operand of MMA 2 as two
 // 128-row tiles of K 64 (the first 64 rows of the first tile are MMA 1's
@@ -591,20 +591,17 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                 tc::fence_after_sync();
                 {
                     const uint32_t tacc = tmem + lane_q + T_D + (uint32_t)(b * 128 + tl * 64 + 32 * hc);
-                    uint32_t v[32];
-                    tc::tmem_ld16(tacc, *reinterpret_cast<uint32_t(*)[16]>(v));
-                    tc::tmem_ld16(tacc + 16, *reinterpret_cast<uint32_t(*)[16]>(v + 16));
-                    tc::tmem_ld_wait();
                     const uint32_t zbase = sbase + OFF_P + (uint32_t)(b * 2 + hc) * TILE;
 #pragma unroll
                     for (int hh = 0; hh < 2; hh++) {
-                        uint32_t tv[16];
+                        uint32_t v[16], tv[16];
+                        tc::tmem_ld16(tacc + (uint32_t)(16 * hh), v);
                         tc::tmem_ld16(ttw + (uint32_t)(16 * hh), tv);
                         tc::tmem_ld_wait();
 #pragma unroll
                         for (int k = 0; k < 8; k++) {
                             const int kk = 8 * hh + k;
-                            const float yr = __uint_as_float(v[2 * kk]), yi = __uint_as_float(v[2 * kk + 1]);
+                            const float yr = __uint_as_float(v[2 * k]), yi = __uint_as_float(v[2 * k + 1]);
                             const float tr = __uint_as_float(tv[2 * k]), ti = __uint_as_float(tv[2 * k + 1]);
                             const float zr = fmaf(yr, tr, -yi * ti);
                             const float zi = fmaf(yr, ti, yi * tr);
