@@ -60,8 +60,8 @@ NCU_TRAFFIC_C2 = {"fengine_c64b": 677.995e6 + 2637.297e6,
 # Nsp = 1024 (profiles/fengine_tc_c3.txt, profiles/xengine_tc_c3.txt): the
 # F-engine's reads and writes and the X-engine's operand reads grow with the
 # spectra processed, the X-engine's visibility writes do not.
-NCU_TRAFFIC_C3 = {"fengine_tc": 0.551991e9 * 8199 / 1031 + 1.021304e9 * 8,
-                  "xengine_tc": 1.076980e9 * 8 + 0.484042e9}
+NCU_TRAFFIC_C3 = {"fengine_tc": 0.544354e9 * 8199 / 1031 + 1.025016e9 * 8,
+                  "xengine_tc": 1.075430e9 * 8 + 0.488982e9}
 
 
 def bind_to_gpu_cpus(gpu_index):
