@@ -240,7 +240,7 @@ def measure_plan(mdt, cfg, precision, dev, steps, warmup, iq=None, win=None):
     return ms, f_ms / max(count, 1), x_ms / max(count, 1), scale
 
 
-def kernel_roofline(cfg, precision, f_ms, x_ms, sm_mhz, nsm):
+def kernel_roofline(cfg, precision, f_ms, x_ms, sm_mhz, nsm, fp32_peak=None):
     """Per-kernel figures of one integration: (kernels dict, roofline of the
     slower one).  Bytes per launch: F-engine reads 2 B per input sample
     (Nsp + Ntaps - 1 spectra) and writes its output layout (8 B per sample
@@ -257,6 +257,10 @@ def kernel_roofline(cfg, precision, f_ms, x_ms, sm_mhz, nsm):
         xpeak = nsm * 128 * 2 * (sm_mhz or 1900.0) * 1e6 / 1e12
         xpeak_src = ("nominal FP32 FMA rate (%d SMs x 128 lanes x 2) at the sampled SM clock"
                      % nsm)
+        if fp32_peak:
+            xpeak = fp32_peak
+            xpeak_src = ("measured FP32 FMA rate (mdt_fp32_peak: one 1024-thread CTA per SM, "
+                         "independent FMA chains, the faster of packed f32x2 and scalar)")
         traffic = NCU_TRAFFIC_C2 if cfg.name == "c2_station40" else {}
     else:
         nep, nkc = (ne + 15) // 16 * 16, (nsp + 31) // 32
@@ -771,10 +775,15 @@ def station_section(mdt, dev, steps, barrier, local, with_e2e):
     win = make_window(mdt, c2, dev)
     ms, f, x, _ = measure_plan(mdt, c2, 0, dev, steps=steps, warmup=2, iq=iq, win=win)
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
-    kernels, roof = kernel_roofline(c2, "fp32", f, x, 2070.0, nsm)
+    _, fp32_packed = mdt.fp32_peak(True)
+    _, fp32_scalar = mdt.fp32_peak(False)
+    kernels, roof = kernel_roofline(c2, "fp32", f, x, 2070.0, nsm,
+                                    fp32_peak=max(fp32_packed, fp32_scalar))
     res = {"workload": c2.name, "precision": "fp32", "value": c2.antenna_samples() / (ms * 1e-3),
            "unit": "antenna-samples/s", "ms_per_step": ms, "integrations": c2.nint,
-           "kernels": kernels, "roofline": roof}
+           "kernels": kernels, "roofline": roof,
+           "fp32_peaks": {"fma_f32x2": fp32_packed, "fma_f32": fp32_scalar,
+                          "nominal": nsm * 128 * 2 * 2070.0e6 / 1e12, "unit": "TFLOP/s"}}
     if with_e2e:
         r = e2e_run(mdt, c2, "fp32", dev, iq, None, c2.antenna_samples(), 5, barrier, local)
         res["e2e"] = {"value": c2.antenna_samples() / r.pop("median_s"),

@@ -192,6 +192,14 @@ MDT_API mdt_status mdt_fengine_tc_q8(int ne, int nch, int ntaps, int nsp, const 
 MDT_API mdt_status mdt_tc_peak_f16(int n, int ctas_per_sm, int iters, int reps, float *best_ms,
                                    double *tflops, int *err, cudaStream_t stream);
 
+/* Measured FP32 FMA throughput: one 1024-thread CTA per SM, each thread
+ * running independent FMA chains of `iters` steps (packed fma.rn.f32x2 when
+ * `packed`, else scalar fma.rn.f32); the best of `reps` timed launches
+ * (after one warm-up) gives *best_ms and *tflops (2 flops per FMA).
+ * Measurement support: the denominator for the FP32 X-engine's fraction. */
+MDT_API mdt_status mdt_fp32_peak(int packed, int iters, int reps, float *best_ms, double *tflops,
+                                 cudaStream_t stream);
+
 /* Exact-int8 F-engine: as mdt_fengine_x16 but the values are integers
  * clamp(rint(x * qscales[c]), -127, 127) (stored as f16, exactly). */
 MDT_API mdt_status mdt_fengine_q8(int ne, int nch, int ntaps, int nsp, const int8_t *iq,

@@ -25,7 +25,7 @@ from .binding import (  # noqa: F401
     window_hamming_sinc, fft_c2c, xengine_f32, fengine_f32, synth_iq,
     fengine_x16, xengine_tc, x16_bytes, fengine_c64b, fx_integrate_static,
     FxPlan, FxBatch, MDT_PREC_FP32, MDT_PREC_FP16, MDT_PREC_BF16, MDT_PREC_INT8,
-    fengine_q8, xengine_q8, fengine_tc, fengine_tc_q8, tc_peak_f16,
+    fengine_q8, xengine_q8, fengine_tc, fengine_tc_q8, tc_peak_f16, fp32_peak,
     apply_gains, xengine_adjoint_f32, gain_adjoint, pfb_tap_grad,
     PacketFormat, packet_format, depacketise_seen_words, depacketise, depacketise_finish,
     STATS_FIELDS, Ingest, num_baselines, format_baselines, write_csv, write_binary,

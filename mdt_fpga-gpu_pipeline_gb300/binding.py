@@ -76,6 +76,8 @@ def _declare(L):
         "mdt_fengine_q8": ([_I, _I, _I, _I, _P, _P, _P, _P, _P], _I),
         "mdt_tc_peak_f16": ([_I, _I, _I, _I, ctypes.POINTER(ctypes.c_float),
                              ctypes.POINTER(ctypes.c_double), _P, _P], _I),
+        "mdt_fp32_peak": ([_I, _I, _I, ctypes.POINTER(ctypes.c_float),
+                           ctypes.POINTER(ctypes.c_double), _P], _I),
         "mdt_xengine_q8": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P], _I),
         "mdt_fx_integrate_static": ([_I, _I, _I, _I, _P, _P, _P, _P], _I),
         "mdt_fx_get_scale": ([_P, ctypes.POINTER(ctypes.c_float)], _I),
@@ -308,6 +310,15 @@ def fengine_tc(ne, nch, ntaps, nsp, iq, window, X16, err, ab_fmt=0, scale=1.0, s
     """Tensor-core F-engine (Nch 1024): same output layout as fengine_x16."""
     check(lib().mdt_fengine_tc(ne, nch, ntaps, nsp, ptr(iq), ptr(window), ptr(X16), ab_fmt, scale,
                                ptr(err), stream_handle(stream)), "fengine_tc")
+
+
+def fp32_peak(packed=True, iters=100000, reps=5, stream=None):
+    """Measured FP32 FMA throughput (best of `reps` launches): (ms, TFLOP/s)."""
+    ms = ctypes.c_float(0.0)
+    tf = ctypes.c_double(0.0)
+    check(lib().mdt_fp32_peak(1 if packed else 0, iters, reps, ctypes.byref(ms), ctypes.byref(tf),
+                              stream_handle(stream)), "fp32_peak")
+    return ms.value, tf.value
 
 
 def tc_peak_f16(n=256, ctas_per_sm=1, iters=20000, reps=5, err=None, stream=None):

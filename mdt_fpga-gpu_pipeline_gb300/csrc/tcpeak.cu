@@ -2,6 +2,8 @@
 // operands, FP32 accumulate, M = 128, K = 16, N = 128 or 256) with both
 // operands resident in shared memory: the tensor-core ceiling the X-engine's
 // instruction shape can reach on this GPU, measured rather than quoted.
+// Also the FP32 FMA rate (packed fma.rn.f32x2 or scalar fma.rn.f32), the
+// ceiling of the FP32 SIMT X-engine.
 //
 // Each CTA fills a 128-row A tile and an N-row B tile (K = 64 f16, the
 // 128-byte-swizzled K-major layout the X-engine uses) with pseudo-random
@@ -72,7 +74,90 @@ __global__ void __launch_bounds__(PK_THREADS, 1) tc_peak_kernel(int n, int iters
     }
 }
 
+constexpr int FP_THREADS = 1024;
+
+// Each thread runs 8 independent chains of packed FP32 FMAs (PACKED) or 16
+// of scalar ones, `iters` steps each: 32 flops per thread and step either way.
+template <bool PACKED>
+__global__ void __launch_bounds__(FP_THREADS, 1) fp32_peak_kernel(int iters, float *sink)
+{
+    const float t = (float)(threadIdx.x + blockIdx.x * FP_THREADS) * 1e-7f;
+    float s = 0.0f;
+    if constexpr (PACKED) {
+        float2 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = make_float2(t + (float)k, t - (float)k);
+        const float2 m = make_float2(0.99999f, 1.00001f), c = make_float2(1e-6f, -1e-6f);
+        for (int it = 0; it < iters; it++) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = __ffma2_rn(v[k], m, c);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) s += v[k].x + v[k].y;
+    } else {
+        float v[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) v[k] = t + (float)k;
+        for (int it = 0; it < iters; it++) {
+#pragma unroll
+            for (int k = 0; k < 16; k++) v[k] = __fmaf_rn(v[k], 0.99999f, 1e-6f);
+        }
+#pragma unroll
+        for (int k = 0; k < 16; k++) s += v[k];
+    }
+    if (s == -1.0e30f) *sink = s;  // keeps the chains live; never true for these values
+}
+
 }  // namespace mdt
+
+// Times `reps` launches of one 1024-thread CTA per SM running the FMA chains
+// above; returns the best launch's time and its TFLOP/s (2 flops per FMA).
+extern "C" MDT_API mdt_status mdt_fp32_peak(int packed, int iters, int reps, float *best_ms,
+                                            double *tflops, cudaStream_t stream)
+{
+    if (iters < 1 || reps < 1 || !best_ms || !tflops) return mdt::invalid("fp32_peak: bad arguments");
+    float *sink = nullptr;
+    cudaError_t e = cudaMalloc(&sink, sizeof(float));
+    if (e != cudaSuccess) return mdt::cuda_status(e, "fp32_peak alloc");
+    const unsigned grid = (unsigned)mdt::sm_count();
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess) {
+        cudaFree(sink);
+        return mdt::cuda_status(cudaGetLastError(), "fp32_peak event");
+    }
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        cudaFree(sink);
+        return mdt::cuda_status(cudaGetLastError(), "fp32_peak event");
+    }
+    float best = 0.0f;
+    mdt_status st = MDT_SUCCESS;
+    for (int r = 0; r <= reps && st == MDT_SUCCESS; r++) {  // launch 0 warms up
+        cudaEventRecord(a, stream);
+        if (packed)
+            mdt::fp32_peak_kernel<true><<<grid, mdt::FP_THREADS, 0, stream>>>(iters, sink);
+        else
+            mdt::fp32_peak_kernel<false><<<grid, mdt::FP_THREADS, 0, stream>>>(iters, sink);
+        st = mdt::launch_status("fp32_peak_kernel");
+        cudaEventRecord(b, stream);
+        if (st != MDT_SUCCESS) break;
+        e = cudaEventSynchronize(b);
+        if (e != cudaSuccess) {
+            st = mdt::cuda_status(e, "fp32_peak sync");
+            break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (r > 0 && (best == 0.0f || ms < best)) best = ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (st != MDT_SUCCESS) return st;
+    *best_ms = best;
+    *tflops = 32.0 * iters * (double)mdt::FP_THREADS * grid / (best * 1e-3) / 1e12;
+    return MDT_SUCCESS;
+}
 
 // Times `reps` launches of ctas_per_sm CTAs per SM, each issuing `iters` x 4
 // MMAs of 128 x n x 16; returns the best launch's time and its TFLOP/s

@@ -54,16 +54,18 @@ namespace mdt {
 constexpr int TC_STAGES = 4;
 constexpr int TC_BROWS = 256;  // max column-chunk rows (N)
 constexpr int TC_AROWS = 128;  // row tile (M)
-constexpr int TC_THREADS = 192;
-// threads of a KIND 0 block (producer, MMA, 4 epilogue warps) or a KIND 1
-// block (producer, MMA, 16 epilogue warps holding the int32 running sums)
-constexpr int tc_threads(int kind) { return kind == 1 ? 576 : TC_THREADS; }
+constexpr int TC_THREADS = 192;  // the batched kernel: producer, MMA, 4 epilogue warps
+// threads of a KIND 0 block (producer, MMA, 8 epilogue warps: two per TMEM lane
+// quarter, each on half of the columns) or a KIND 1 block (producer, MMA, 16
+// epilogue warps holding the int32 running sums)
+constexpr int tc_threads(int kind) { return kind == 1 ? 576 : 320; }
 constexpr int TC_MAX_TILES = 160;
 constexpr uint32_t TC_A_BYTES = TC_AROWS * 128;
 // Epilogue scratch of the f16/bf16 kernel with 128-wide chunks, reused from the
-// stage ring once every MMA has completed: the per-warp 32 x 33 transpose
-// blocks of the conjugate mirror, then a diagonal tile's G (128 rows of 129
-// floats, the odd stride keeping row and column accesses conflict-free).
+// stage ring once every MMA has completed: the conjugate mirror's transpose
+// blocks (16 columns x 33 rows per epilogue warp, or 32 x 33 for each of the
+// batched kernel's four), then a diagonal tile's G (128 rows of 129 floats,
+// the odd stride keeping row and column accesses conflict-free).
 constexpr int TC_GS = 129;
 constexpr size_t TC_TB_BYTES = 4 * 32 * 33 * sizeof(float2);
 constexpr size_t TC_GS_BYTES = (size_t)TC_AROWS * TC_GS * sizeof(float);
@@ -295,70 +297,67 @@ __global__ void __launch_bounds__(tc_threads(KIND), (KIND == 0 && BROWS == 128 ?
         }
         if (!ok && lane == 0) atomicExch(a.err, 1);
     } else if (warp >= 2 && KIND == 0) {
-        // ---------------- epilogue: TMEM -> visibilities
+        // ---------------- epilogue: TMEM -> visibilities, 8 warps: warp w reads
+        // TMEM lane quarter w % 4 and the columns of half (w - 2) / 4
         ok = tc::mbar_wait_sleep(tc::smem_u32(&bars[2 * STAGES]), 0);
         tc::fence_after_sync();
-        const int quarter = warp & 3;
+        const int quarter = warp & 3, half = (warp - 2) >> 2;
         const int r = tile.r0 + quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
         float2 *Vc = a.V ? a.V + (long)ch * a.ne * a.ne : nullptr;
         double2 *Ac = a.Vacc ? a.Vacc + (long)ch * a.ne * a.ne : nullptr;
+        // this warp's columns [c0, c1): N is a multiple of 16, halves are too
+        const int nh = ((N + 31) / 32) * 16;
+        const int c0 = half * nh, c1 = min(N, c0 + nh);
         // The lower triangle V[q*NE + r] is written along r (the lanes).  The
         // conjugate mirror V[r*NE + q] is transposed through shared memory (the
-        // stage ring is idle once every MMA has completed) in 32 x 32 blocks
-        // so that it is written along q as well.
-        float2 *tb = reinterpret_cast<float2 *>(smem) + (size_t)quarter * 32 * 33;  // [q][r]
+        // stage ring is idle once every MMA has completed) in 16-column blocks
+        // so that it is written along q as well, two rows per store.
+        float2 *tb = reinterpret_cast<float2 *>(smem) + (size_t)(warp - 2) * 16 * 33;  // [q][r]
         const int rbase = tile.r0 + quarter * 32;
         // diagonal tile: G (the Im accumulator) row by row into shared memory, so
         // that each thread can read the transposed entry G[q][r] (tile-local)
         float *gs = reinterpret_cast<float *>(smem + TC_TB_BYTES);
         const int rl = quarter * 32 + lane;
         if (sym) {
-            for (int n0 = 0; n0 < N; n0 += 16) {
+            for (int n0 = c0; n0 < c1; n0 += 16) {
                 uint32_t vg[16];
                 tc::tmem_ld16(d_im + lane_off + n0, vg);
                 tc::tmem_ld_wait();
 #pragma unroll
-                for (int j = 0; j < 16; j++)
-                    if (n0 + j < N) gs[rl * TC_GS + n0 + j] = __uint_as_float(vg[j]);
+                for (int j = 0; j < 16; j++) gs[rl * TC_GS + n0 + j] = __uint_as_float(vg[j]);
             }
         }
-        if (tc_sym(KIND, BROWS)) tc::named_barrier(1, 128);  // the four epilogue warps
-        for (int n0 = 0; n0 < N; n0 += 32) {
+        if (tc_sym(KIND, BROWS)) tc::named_barrier(1, 256);  // the eight epilogue warps
+        for (int n0 = c0; n0 < c1; n0 += 16) {
+            uint32_t vr[16], vi[16];
+            tc::tmem_ld16(d_re + lane_off + n0, vr);
+            tc::tmem_ld16(d_im + lane_off + n0, vi);
+            tc::tmem_ld_wait();
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                uint32_t vr[16], vi[16];
-                const bool has = n0 + 16 * h < N;
-                if (has) {
-                    tc::tmem_ld16(d_re + lane_off + n0 + 16 * h, vr);
-                    tc::tmem_ld16(d_im + lane_off + n0 + 16 * h, vi);
-                    tc::tmem_ld_wait();
-                }
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const int q = tile.q0 + n0 + 16 * h + j;
-                    const bool live = has && ok && r < a.ne && q < a.ne && q <= r;
-                    const float re = live ? __uint_as_float(vr[j]) * a.alpha : 0.0f;
-                    const float g = sym && live ? gs[(n0 + 16 * h + j) * TC_GS + rl] : 0.0f;
-                    const float im = (live && q != r) ? (__uint_as_float(vi[j]) - g) * a.alpha : 0.0f;
-                    tb[(16 * h + j) * 33 + lane] = make_float2(re, -im);
-                    if (!live) continue;
-                    const long lo = (long)q * a.ne + r;
-                    if (Vc) Vc[lo] = make_float2(re, im);
-                    if (Ac) {
-                        double2 x = Ac[lo];
-                        Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
-                    }
+            for (int j = 0; j < 16; j++) {
+                const int q = tile.q0 + n0 + j;
+                const bool live = ok && r < a.ne && q < a.ne && q <= r;
+                const float re = live ? __uint_as_float(vr[j]) * a.alpha : 0.0f;
+                const float g = sym && live ? gs[(n0 + j) * TC_GS + rl] : 0.0f;
+                const float im = (live && q != r) ? (__uint_as_float(vi[j]) - g) * a.alpha : 0.0f;
+                tb[j * 33 + lane] = make_float2(re, -im);
+                if (!live) continue;
+                const long lo = (long)q * a.ne + r;
+                if (Vc) Vc[lo] = make_float2(re, im);
+                if (Ac) {
+                    double2 x = Ac[lo];
+                    Ac[lo] = make_double2(x.x + (double)re, x.y + (double)im);
                 }
             }
             __syncwarp();
-            // mirror: row r = rbase + rr, columns q = tile.q0 + n0 + lane (q < r)
-            const int q = tile.q0 + n0 + lane;
+            // mirror: rows rbase + rr (two per step), columns q = tile.q0 + n0 + (lane & 15)
+            const int qc = lane & 15, q = tile.q0 + n0 + qc;
 #pragma unroll 4
-            for (int rr = 0; rr < 32; rr++) {
-                const int rm = rbase + rr;
-                if (!ok || rm >= a.ne || q >= a.ne || q >= rm || n0 + lane >= N) continue;
-                const float2 v = tb[lane * 33 + rr];
+            for (int i = 0; i < 16; i++) {
+                const int rr = 2 * i + (lane >> 4), rm = rbase + rr;
+                if (!ok || rm >= a.ne || q >= a.ne || q >= rm) continue;
+                const float2 v = tb[qc * 33 + rr];
                 const long up = (long)rm * a.ne + q;
                 if (Vc) Vc[up] = v;
                 if (Ac) {
@@ -629,7 +628,7 @@ mdt_status xengine_tc(int ne, int nch, int nsp, const void *X16, int ab_fmt, flo
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return cuda_status(e, "xengine_tc smem attribute");
-        kern<<<(unsigned)blocks, TC_THREADS, smem, stream>>>(a);
+        kern<<<(unsigned)blocks, tc_threads(0), smem, stream>>>(a);
         return launch_status("xengine_tc_kernel");
     };
     return wide ? launch(xengine_tc_kernel<0, 256, 4>, tc_smem(0, 256, 4))

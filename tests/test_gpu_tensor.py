@@ -160,3 +160,14 @@ def test_tc_peak_f16_microbenchmark(mdt, cuda):
         print("kind::f16 M128 N%d, %d CTA/SM: %.1f TFLOP/s (%.3f ms)" % (n, per_sm, tflops, ms))
         assert int(err.item()) == 0
         assert 225.0 < tflops < 2580.0
+
+
+def test_fp32_peak_microbenchmark(mdt, cuda):
+    """The FP32 FMA throughput measurement runs for both instruction forms and
+    lands between a tenth of the 152 SMs x 128 lanes x 2 flops at 2.07 GHz
+    (80.5 TFLOP/s) and twice that figure (a packed f32x2 FMA might retire two
+    lanes' worth per lane and cycle)."""
+    for packed in (True, False):
+        ms, tflops = mdt.fp32_peak(packed, iters=20000, reps=2)
+        print("FP32 FMA (%s): %.1f TFLOP/s (%.3f ms)" % ("f32x2" if packed else "f32", tflops, ms))
+        assert 8.0 < tflops < 161.0
