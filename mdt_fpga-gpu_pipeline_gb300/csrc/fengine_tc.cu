@@ -407,7 +407,6 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     }
                     tc::tmem_st16(carry_t + (uint32_t)(16 * j), cv);
                 }
-                tc::tmem_st_wait();
                 tc::mbar_arrive(bar(BAR_EMPTY + slot));
                 r++;
             }
@@ -421,6 +420,7 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     ok = false;
                     break;
                 }
+                tc::tmem_st_wait();  // the previous unit's (or lead-in's) carry stores
                 const uint32_t gP = sbase + OFF_P + (uint32_t)b * 2 * TILE;
                 // ---- PFB: 8 spectra x 4 channels per thread -> P tiles (f16, scaled)
 #pragma unroll
@@ -463,12 +463,12 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
                     }
                     tc::tmem_st16(carry_t + (uint32_t)(16 * j), cv);
                 }
-                tc::tmem_st_wait();  // the next unit reads the carry back
                 tc::mbar_arrive(bar(BAR_EMPTY + slot));  // the ring slot may be refilled
                 tc::fence_proxy_async();                 // P is read by the tensor cores
                 tc::mbar_arrive(bar(BAR_PFULL + b));
             }
         }
+        tc::tmem_st_wait();  // no carry store in flight when the CTA frees TMEM
     } else if (tid < PT + ET) {
         // ======================================================= epilogue role
         // 16 warps.  Twiddle stage: warp 8 + ew reads TMEM lane quarter
@@ -548,12 +548,12 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
             const bool last = nvalid <= US;  // the element's last unit
             const uint32_t stash = tmem + lane_q + T_STASH + (uint32_t)(16 * cb);
             if (!second && !last) {
-                tc::tmem_st16(stash, q);
-                tc::tmem_st_wait();
+                tc::tmem_st16(stash, q);  // waited for before the second unit reads it
                 return true;
             }
             uint32_t f[16];
             if (second) {
+                tc::tmem_st_wait();
                 tc::tmem_ld16(stash, f);
                 tc::tmem_ld_wait();
             }
@@ -623,6 +623,7 @@ __global__ void __launch_bounds__(THREADS, 1) fengine_tc_kernel(Launch L)
             }
         }
         if (ok && have_pend && !output(n - 1, pend)) fail();
+        tc::tmem_st_wait();  // no stash store in flight when the CTA frees TMEM
     } else if (tid == PT + ET) {
         // ========================================================= loader role
         long total_uses = 0;  // this CTA's ring uses: one lead-in per work item, then its units
