@@ -40,8 +40,8 @@
 //
 // Warp roles: warp 0 lane 0 issues bulk copies into the shared-memory stage
 // ring; warp 1 allocates tensor memory and its lane 0 issues the MMAs and
-// commits; the epilogue warps (2-5, or 2-17 in the exact int8 mode) read the
-// accumulators and write visibilities.  Every mbarrier wait is bounded; a
+// commits; the epilogue warps (2-9, two per TMEM lane quarter, or 2-17 in the
+// exact int8 mode) read the accumulators and write visibilities.  Every mbarrier wait is bounded; a
 // timeout sets the error flag and the block finishes without further work.
 #include <cstdlib>
 
